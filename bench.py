@@ -1,0 +1,356 @@
+"""Benchmark: iiwa_14 forward-dynamics gradients on GB300.
+
+Workload (one "step"): the ragged 512-trajectory mix -- horizons ~ U{8..256}
+(seed 2021, 67.6k knots), knots q ~ U(URDF joint limits), qd ~ U(-2, 2),
+u ~ U(-20, 20) (seeded synthetic data; the reference ships no dataset) --
+through the full path (RNEA, Minv, q̈, dtau/dq, dtau/dqd, -Minv dtau) in FP32.
+
+  value     knot-gradients/s of the batched form: one persistent launch over
+            the ragged offset list, replayed as a CUDA graph, inputs resident
+            in HBM; 6 rotating input/output sets (~280 MB > 129 MB L2).
+  e2e       the same metric through the C ABI's host-buffer call
+            (frg_gradient_host): H2D of q, qd, u from pinned memory, kernel,
+            D2H of dqdd, qdd, Minv inside every timed step.
+  plain     the plain form of the same mix: one launch per trajectory.
+  served    p50/p99 request latency of the continuous-batching server.
+  roofline  dominant kernel (the batched kernel): algorithmic bytes
+            (84 B in + 616 B out per knot) / CUDA-event launch time vs the
+            measured HBM copy peak; FP32 work at the reference's 35,257
+            FLOP/knot vs the FP32 CUDA-core peak.
+
+--impl reference times the reference algorithm's CPU path (the oracle's C
+restatement, threaded like time_CPU.cpp) on this host's cores on the same
+workload.  Under torchrun each rank runs its own mix (weak scaling); there is
+no collective on the data path.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "fast-rbd-gradients_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "knot-pt gradients/s + p99 request latency, batched/served vs plain, same GB300"
+UNIT = "knot-gradients/s"
+N_TRAJ, H_LO, H_HI, MIX_SEED = 512, 8, 256, 2021
+BYTES_PER_KNOT = 84 + 616          # algorithmic HBM bytes: q, qd, u in; dqdd, qdd, Minv out
+FLOP_PER_KNOT_REF = 35257          # the reference's full path as written (op-counted)
+ROTATING_SETS = 6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["frg", "reference"], default="frg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving latency measurement")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(rank):
+    import frg
+    h, off = frg.ragged_horizons(N_TRAJ, H_LO, H_HI, seed=MIX_SEED + rank)
+    n = int(off[-1])
+    q, qd, u = frg.sample_knots(n, seed=MIX_SEED * 7 + rank)
+    return h, off, n, q, qd, u
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return pk, "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def ncu_traffic_per_knot():
+    """DRAM bytes per knot of the batched kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "grad_ragged_kernel_mix512.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_knot:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": len(self.rows)}
+        if not self.rows:
+            return out
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in self.rows if num(r[1])]
+        mx = [num(r[2]) for r in self.rows if num(r[2])]
+        if sm:
+            out["sm_mhz"] = statistics.median(sm)
+        if mx:
+            out["sm_max_mhz"] = max(mx)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for i, nm in enumerate(names):
+            if any(r[5 + i].lower() == "active" for r in self.rows):
+                out["reasons"].append(nm)
+        return out
+
+
+def cpu_baseline(q, qd, u, budget_s=8.0):
+    """The oracle port (C restatement of the reference CPU path) on all host
+    threads, on a bounded sample of the workload's knots."""
+    import frg_oracle
+    threads = os.cpu_count() or 1
+    m = min(len(q), 16384)
+    qs, qds, us = q[:m], qd[:m], u[:m]
+    t, _ = frg_oracle.time_threaded_f32(qs, qds, us, threads, 1)  # warm
+    iters = max(1, int(budget_s / max(t, 1e-3)))
+    t, _ = frg_oracle.time_threaded_f32(qs, qds, us, threads, iters)
+    frg_oracle.shutdown_pool()
+    return {"value": m * iters / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{m} knots of the mix x {iters} rounds ({t:.1f} s), FP32, damping off, gravity on"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    import frg_oracle
+    h, off, n, q, qd, u = workload(0)
+    threads = os.cpu_count() or 1
+    for _ in range(max(args.warmup, 1)):
+        frg_oracle.time_threaded_f32(q, qd, u, threads, 1)
+    t, _ = frg_oracle.time_threaded_f32(q, qd, u, threads, args.steps)
+    frg_oracle.shutdown_pool()
+    value = n * args.steps / t
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"ragged mix: {N_TRAJ} trajectories, horizons U{{{H_LO}..{H_HI}}}, {n} knots",
+                   "knots_per_step": n, "path": "CPU: oracle C restatement of helpers_CPU, persistent thread pool"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"full mix ({n} knots) per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_frg(args):
+    import torch
+    import frg
+
+    ws, rank, local = dist_setup()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+    h, off, n, q, qd, u = workload(rank)
+    peaks, peaks_src = load_peaks()
+
+    ctx = frg.Context(device=dev.index)
+    tuned = ctx.autotune(n)
+    shape = ctx.launch_shape()
+
+    stream = torch.cuda.Stream(device=dev)
+    sets = []
+    with torch.cuda.stream(stream):
+        for i in range(ROTATING_SETS):
+            qq = frg.perturb(q, 1e-3, seed=i) if i else q
+            tq, tqd, tu = (torch.from_numpy(x).to(dev) for x in (qq, qd, u))
+            outs = (torch.empty((n, 98), device=dev), torch.empty((n, 7), device=dev), torch.empty((n, 49), device=dev))
+            plan = ctx.plan_ragged(off, tq, tqd, tu, *outs)
+            o = [int(x) for x in off]
+            trajs = [(o[t + 1] - o[t], tq[o[t]:], tqd[o[t]:], tu[o[t]:], outs[0][o[t]:], outs[1][o[t]:],
+                      outs[2][o[t]:]) for t in range(N_TRAJ)]
+            sets.append((tq, tqd, tu, outs, plan, trajs))
+    stream.synchronize()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    def timed(fn, steps):
+        """Per-step CUDA-event times (ms) on `stream` for `steps` calls."""
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i in range(steps):
+            evs[i][0].record(stream)
+            fn(i)
+            evs[i][1].record(stream)
+        stream.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
+
+    # ---- batched (value) ----
+    # clocks are sampled over a load window: >= 1.5 s of back-to-back warm-up
+    # launches (at least W of them) followed by the K timed steps
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    i, tw = 0, time.perf_counter()
+    while i < args.warmup or time.perf_counter() - tw < 1.5:
+        sets[i % ROTATING_SETS][4].launch(stream)
+        i += 1
+        if i % 64 == 0:
+            stream.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    step_ms = timed(lambda i: sets[i % ROTATING_SETS][4].launch(stream), args.steps)
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    total_ms = sum(step_ms)
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = n * ws * args.steps / (total_ms * 1e-3)
+
+    # ---- plain per-trajectory launches ----
+    for i in range(args.warmup):
+        ctx.per_trajectory(sets[i % ROTATING_SETS][5], stream)
+    plain_ms = timed(lambda i: ctx.per_trajectory(sets[i % ROTATING_SETS][5], stream), max(5, args.steps // 5))
+    plain_value = n / (statistics.mean(plain_ms) * 1e-3)
+
+    # ---- e2e through the C ABI with host buffers ----
+    hq, hqd, hu = (frg.lib().frg_host_alloc(7 * 4 * n) for _ in range(3))
+    hout = [frg.lib().frg_host_alloc(w * 4 * n) for w in (98, 7, 49)]
+    for ptr, arr in ((hq, q), (hqd, qd), (hu, u)):
+        np.ctypeslib.as_array((ctypes.c_float * (7 * n)).from_address(ptr))[:] = arr.reshape(-1)
+    for _ in range(max(1, args.warmup)):
+        ctx.gradient_host_into(n, hq, hqd, hu, *hout)
+    e2e_steps = max(5, args.steps // 5)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.gradient_host_into(n, hq, hqd, hu, *hout)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    for p in [hq, hqd, hu] + hout:
+        frg.lib().frg_host_free(p)
+
+    # ---- serving latency ----
+    served = None
+    if not args.no_serve:
+        try:
+            from frg import serve
+            served = serve.bench_latency(ctx, seconds=4.0)
+        except (ImportError, AttributeError):
+            served = None
+
+    line = None
+    if rank == 0:
+        launch_ms = statistics.mean(step_ms)
+        achieved_gbs = BYTES_PER_KNOT * n / (launch_ms * 1e-3) / 1e9
+        traffic_pk = ncu_traffic_per_knot()
+        sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+        props = torch.cuda.get_device_properties(dev)
+        fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+        fp32_achieved = FLOP_PER_KNOT_REF * n / (launch_ms * 1e-3) / 1e12
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {
+                "workload": f"ragged mix: {N_TRAJ} trajectories, horizons U{{{H_LO}..{H_HI}}} (seed {MIX_SEED}), "
+                            f"{n} knots per rank; batched persistent launch replayed as a CUDA graph",
+                "knots_per_step": n, "l2": f"{ROTATING_SETS} rotating input/output sets "
+                                            f"({ROTATING_SETS * n * BYTES_PER_KNOT / 1e6:.0f} MB > 129 MB L2)",
+                "launch_shape": {"warps_per_cta": shape[0], "ctas_per_sm": shape[1]},
+                "autotune_knots_per_s": tuned, "parallelism": f"replicas x{ws} (knots sharded, no collective)",
+            },
+            "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 84 * n, "d2h_bytes_per_step": 616 * n,
+                    "call": "frg_gradient_host (pinned host buffers)"},
+            "plain_per_trajectory": {"value": plain_value, "unit": UNIT, "launches_per_step": N_TRAJ,
+                                     "ms_per_step": statistics.mean(plain_ms)},
+            "batched_vs_plain": value / ws / plain_value,
+            "served": served,
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
+                         "frac": achieved_gbs / float(peaks["hbm_gbs"]),
+                         "traffic": (traffic_pk * n) if traffic_pk else None,
+                         "peak_source": f"{peaks_src} (MEASURED_PEAKS.json hbm_gbs)" if peaks_src == "measured"
+                         else "fallback 6.8 TB/s", "bytes_per_knot": BYTES_PER_KNOT,
+                         "kernel": "grad_ragged_kernel", "launch_ms": launch_ms},
+            "compute_roofline": {"bound": "fp32", "achieved": fp32_achieved, "unit": "TFLOP/s",
+                                 "peak": fp32_peak, "frac": fp32_achieved / fp32_peak,
+                                 "flop_per_knot": FLOP_PER_KNOT_REF,
+                                 "peak_source": "SMs x 128 FP32 lanes x 2 x sm_max_mhz (nominal)"},
+            "clocks": dict(clk, window="warm-up (>= 1.5 s of launches) + timed steps"),
+            "wall_s_timed_region": wall,
+            "gpu_launches": args.steps,
+        }
+    if not args.no_cpu_baseline and rank == 0:
+        line["cpu_baseline"] = cpu_baseline(q, qd, u)
+    for s in sets:
+        s[4].close()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_frg(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

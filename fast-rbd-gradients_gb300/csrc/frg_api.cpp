@@ -1,0 +1,387 @@
+// C ABI of the engine (include/frg.h): contexts, the plain / host / batched
+// calls, plans captured as CUDA graphs, and the launch-shape autotuner.
+#include "frg.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "frg_internal.h"
+#include "frg_kernels.cuh"
+
+using frg::LaunchShape;
+using frg::Segment;
+
+namespace {
+
+thread_local std::string g_orphan_error;  // errors of calls without a context
+
+bool check(frg_ctx *ctx, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return true;
+    frg_set_error(ctx, std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+bool valid_traj(const frg_traj &t) {
+    if (t.n_knots < 0) return false;
+    if (t.n_knots == 0) return true;
+    return t.q && t.qd && t.u && t.dqdd && t.qdd && t.minv;
+}
+
+}  // namespace
+
+void frg_set_error(frg_ctx *ctx, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    else g_orphan_error = msg;
+}
+
+// ----------------------------------------------------------- batch lists ---
+
+bool frg_build_batch(int n_traj, const frg_traj *trajs, HostBatch &hb, std::string &err) {
+    hb.segs.clear();
+    hb.tile_seg.clear();
+    hb.segs.reserve(static_cast<size_t>(n_traj) + 1);
+    long long begin = 0;
+    for (int t = 0; t < n_traj; t++) {
+        const frg_traj &tr = trajs[t];
+        if (!valid_traj(tr)) {
+            err = "trajectory " + std::to_string(t) + ": negative length or null pointer";
+            return false;
+        }
+        hb.segs.push_back(Segment{tr.q, tr.qd, tr.u, tr.dqdd, tr.qdd, tr.minv, begin});
+        begin += tr.n_knots;
+    }
+    hb.segs.push_back(Segment{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, begin});
+    hb.nknots = begin;
+    const long long ntiles = (begin + 31) / 32;
+    if (ntiles > INT_MAX / 2) {
+        err = "batch too large: " + std::to_string(begin) + " knots";
+        return false;
+    }
+    hb.tile_seg.resize(static_cast<size_t>(ntiles));
+    int s = 0;
+    for (long long tile = 0; tile < ntiles; tile++) {
+        const long long g = tile * 32;
+        while (s + 1 < n_traj && hb.segs[s + 1].knot_begin <= g) s++;
+        hb.tile_seg[static_cast<size_t>(tile)] = s;
+    }
+    return true;
+}
+
+bool DeviceBatch::reserve(int nseg_total, int ntiles_cap, std::string &err) {
+    if (nseg_total > seg_cap) {
+        cudaFree(segs);
+        segs = nullptr;
+        seg_cap = 0;
+        if (cudaMalloc(&segs, sizeof(Segment) * static_cast<size_t>(nseg_total)) != cudaSuccess) {
+            err = "cudaMalloc of the segment list failed";
+            return false;
+        }
+        seg_cap = nseg_total;
+    }
+    if (ntiles_cap > tile_cap) {
+        cudaFree(tile_seg);
+        tile_seg = nullptr;
+        tile_cap = 0;
+        if (cudaMalloc(&tile_seg, sizeof(int) * static_cast<size_t>(std::max(ntiles_cap, 1))) != cudaSuccess) {
+            err = "cudaMalloc of the tile list failed";
+            return false;
+        }
+        tile_cap = ntiles_cap;
+    }
+    if (!counter) {
+        if (cudaMalloc(&counter, sizeof(unsigned int)) != cudaSuccess || cudaMemset(counter, 0, sizeof(unsigned int)) != cudaSuccess) {
+            err = "cudaMalloc of the work counter failed";
+            return false;
+        }
+    }
+    return true;
+}
+
+void DeviceBatch::release() {
+    cudaFree(segs);
+    cudaFree(tile_seg);
+    cudaFree(counter);
+    segs = nullptr;
+    tile_seg = nullptr;
+    counter = nullptr;
+    seg_cap = tile_cap = 0;
+}
+
+cudaError_t frg_launch_batch(frg_ctx *ctx, const DeviceBatch &db, int nseg, int ntiles, cudaStream_t stream) {
+    return frg::launch_ragged(ctx->damping, ctx->mpc, ctx->shape, ctx->num_sms, db.segs, nseg, db.tile_seg, ntiles,
+                              db.counter, stream);
+}
+
+// ------------------------------------------------------------------ C ABI ---
+
+extern "C" {
+
+void frg_options_default(frg_options *opt) {
+    if (!opt) return;
+    opt->device = 0;
+    opt->vel_damping = 0;
+    opt->mpc_mode = 0;
+    opt->warps_per_cta = 0;
+    opt->ctas_per_sm = 0;
+}
+
+const char *frg_status_string(frg_status s) {
+    switch (s) {
+        case FRG_OK: return "ok";
+        case FRG_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case FRG_ERR_CUDA: return "CUDA error";
+        case FRG_ERR_OUT_OF_MEMORY: return "out of memory";
+        case FRG_ERR_NOT_READY: return "not ready";
+        case FRG_ERR_ADMISSION: return "request can never be admitted";
+        case FRG_ERR_TIMEOUT: return "timeout";
+        case FRG_ERR_SHUTDOWN: return "shut down";
+        case FRG_ERR_NOT_FOUND: return "not found";
+        case FRG_ERR_INTERNAL: return "internal error";
+    }
+    return "unknown status";
+}
+
+frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
+    if (!out) {
+        frg_set_error(nullptr, "frg_create: out is NULL");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    frg_options opt;
+    frg_options_default(&opt);
+    if (opt_in) opt = *opt_in;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        frg_set_error(nullptr, std::string("frg_create: no CUDA device: ") + cudaGetErrorString(e));
+        return FRG_ERR_CUDA;
+    }
+    if (opt.device < 0 || opt.device >= ndev) {
+        frg_set_error(nullptr, "frg_create: device ordinal out of range");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (opt.warps_per_cta < 0 || opt.warps_per_cta > frg::max_warps_per_cta() || opt.ctas_per_sm < 0) {
+        frg_set_error(nullptr, "frg_create: invalid launch shape");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    frg_ctx *ctx = new (std::nothrow) frg_ctx();
+    if (!ctx) return FRG_ERR_OUT_OF_MEMORY;
+    ctx->device = opt.device;
+    ctx->damping = opt.vel_damping != 0;
+    ctx->mpc = opt.mpc_mode != 0;
+    DeviceGuard g(ctx->device);
+    cudaDeviceProp prop;
+    if (!check(ctx, cudaGetDeviceProperties(&prop, ctx->device), "cudaGetDeviceProperties") ||
+        !check(ctx, frg::init_kernels(), "kernel set-up") ||
+        !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !check(ctx, cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming), "cudaEventCreate")) {
+        g_orphan_error = ctx->err;
+        frg_destroy(ctx);
+        return FRG_ERR_CUDA;
+    }
+    ctx->num_sms = prop.multiProcessorCount;
+    ctx->shape = frg::default_shape();
+    if (opt.warps_per_cta) ctx->shape.warps_per_cta = opt.warps_per_cta;
+    if (opt.ctas_per_sm) ctx->shape.ctas_per_sm = opt.ctas_per_sm;
+    *out = ctx;
+    return FRG_OK;
+}
+
+void frg_destroy(frg_ctx *ctx) {
+    if (!ctx) return;
+    {
+        DeviceGuard g(ctx->device);
+        if (ctx->io_stream) cudaStreamSynchronize(ctx->io_stream);
+        if (ctx->scratch_done) cudaEventSynchronize(ctx->scratch_done);
+        ctx->scratch.release();
+        cudaFree(ctx->host_buf);
+        if (ctx->io_stream) cudaStreamDestroy(ctx->io_stream);
+        if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
+    }
+    delete ctx;
+}
+
+const char *frg_last_error(const frg_ctx *ctx) { return ctx ? ctx->err.c_str() : g_orphan_error.c_str(); }
+
+frg_status frg_set_launch_shape(frg_ctx *ctx, int warps_per_cta, int ctas_per_sm) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (warps_per_cta < 1 || warps_per_cta > frg::max_warps_per_cta() || ctas_per_sm < 1) {
+        frg_set_error(ctx, "frg_set_launch_shape: warps_per_cta must be in [1, 8], ctas_per_sm >= 1");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    ctx->shape.warps_per_cta = warps_per_cta;
+    ctx->shape.ctas_per_sm = ctas_per_sm;
+    return FRG_OK;
+}
+
+frg_status frg_get_launch_shape(const frg_ctx *ctx, int *warps_per_cta, int *ctas_per_sm) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (warps_per_cta) *warps_per_cta = ctx->shape.warps_per_cta;
+    if (ctas_per_sm) *ctas_per_sm = ctx->shape.ctas_per_sm;
+    return FRG_OK;
+}
+
+frg_status frg_gradient(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u, float *dqdd,
+                        float *qdd, float *minv, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 0 || (n_knots > 0 && !(q && qd && u && dqdd && qdd && minv))) {
+        frg_set_error(ctx, "frg_gradient: negative n_knots or null pointer");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n_knots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    if (!check(ctx, frg::launch_plain(ctx->damping, ctx->mpc, ctx->shape, n_knots, q, qd, u, dqdd, qdd, minv, stream),
+               "frg_gradient launch"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                             float *dqdd, float *qdd, float *minv) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 0 || (n_knots > 0 && !(q && qd && u && dqdd && qdd && minv))) {
+        frg_set_error(ctx, "frg_gradient_host: negative n_knots or null pointer");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n_knots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    const size_t n = static_cast<size_t>(n_knots);
+    const size_t need = n * (3 * 7 + 98 + 7 + 49);
+    if (need > ctx->host_buf_floats) {
+        cudaFree(ctx->host_buf);
+        ctx->host_buf = nullptr;
+        ctx->host_buf_floats = 0;
+        if (cudaMalloc(&ctx->host_buf, need * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            frg_set_error(ctx, "frg_gradient_host: cudaMalloc of " + std::to_string(need * 4) + " bytes failed");
+            return FRG_ERR_OUT_OF_MEMORY;
+        }
+        ctx->host_buf_floats = need;
+    }
+    float *dq = ctx->host_buf, *dqd = dq + 7 * n, *du = dqd + 7 * n, *ddqdd = du + 7 * n, *dqdd_ = ddqdd + 98 * n,
+          *dminv = dqdd_ + 7 * n;
+    cudaStream_t s = ctx->io_stream;
+    const size_t b7 = 7 * n * sizeof(float);
+    if (!check(ctx, cudaMemcpyAsync(dq, q, b7, cudaMemcpyHostToDevice, s), "H2D q") ||
+        !check(ctx, cudaMemcpyAsync(dqd, qd, b7, cudaMemcpyHostToDevice, s), "H2D qd") ||
+        !check(ctx, cudaMemcpyAsync(du, u, b7, cudaMemcpyHostToDevice, s), "H2D u") ||
+        !check(ctx, frg::launch_plain(ctx->damping, ctx->mpc, ctx->shape, n_knots, dq, dqd, du, ddqdd, dqdd_, dminv, s),
+               "frg_gradient_host launch") ||
+        !check(ctx, cudaMemcpyAsync(dqdd, ddqdd, 98 * n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H dqdd") ||
+        !check(ctx, cudaMemcpyAsync(qdd, dqdd_, b7, cudaMemcpyDeviceToHost, s), "D2H qdd") ||
+        !check(ctx, cudaMemcpyAsync(minv, dminv, 49 * n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H minv") ||
+        !check(ctx, cudaStreamSynchronize(s), "frg_gradient_host sync"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+frg_status frg_gradient_per_trajectory(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_traj < 0 || (n_traj > 0 && !trajs)) {
+        frg_set_error(ctx, "frg_gradient_per_trajectory: bad trajectory list");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    for (int t = 0; t < n_traj; t++)
+        if (!valid_traj(trajs[t]) || trajs[t].n_knots > INT_MAX) {
+            frg_set_error(ctx, "frg_gradient_per_trajectory: trajectory " + std::to_string(t) + " is invalid");
+            return FRG_ERR_INVALID_ARGUMENT;
+        }
+    DeviceGuard g(ctx->device);
+    for (int t = 0; t < n_traj; t++) {
+        const frg_traj &tr = trajs[t];
+        if (tr.n_knots == 0) continue;
+        if (!check(ctx,
+                   frg::launch_plain(ctx->damping, ctx->mpc, ctx->shape, static_cast<int>(tr.n_knots), tr.q, tr.qd,
+                                     tr.u, tr.dqdd, tr.qdd, tr.minv, stream),
+                   "per-trajectory launch"))
+            return FRG_ERR_CUDA;
+    }
+    return FRG_OK;
+}
+
+frg_status frg_gradient_batched(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_traj < 0 || (n_traj > 0 && !trajs)) {
+        frg_set_error(ctx, "frg_gradient_batched: bad trajectory list");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    HostBatch hb;
+    std::string err;
+    if (!frg_build_batch(n_traj, trajs, hb, err)) {
+        frg_set_error(ctx, "frg_gradient_batched: " + err);
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (hb.nknots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    // the one-shot descriptor buffers are reused: wait for the previous user
+    if (!check(ctx, cudaEventSynchronize(ctx->scratch_done), "scratch wait")) return FRG_ERR_CUDA;
+    const int nseg = n_traj, ntiles = static_cast<int>(hb.tile_seg.size());
+    if (!ctx->scratch.reserve(nseg + 1, ntiles, err)) {
+        cudaGetLastError();
+        frg_set_error(ctx, "frg_gradient_batched: " + err);
+        return FRG_ERR_OUT_OF_MEMORY;
+    }
+    if (!check(ctx,
+               cudaMemcpyAsync(ctx->scratch.segs, hb.segs.data(), sizeof(Segment) * hb.segs.size(),
+                               cudaMemcpyHostToDevice, stream),
+               "segment list upload") ||
+        !check(ctx,
+               cudaMemcpyAsync(ctx->scratch.tile_seg, hb.tile_seg.data(), sizeof(int) * hb.tile_seg.size(),
+                               cudaMemcpyHostToDevice, stream),
+               "tile list upload") ||
+        !check(ctx, frg_launch_batch(ctx, ctx->scratch, nseg, ntiles, stream), "batched launch") ||
+        !check(ctx, cudaEventRecord(ctx->scratch_done, stream), "cudaEventRecord"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+frg_status frg_gradient_ragged(frg_ctx *ctx, int n_traj, const int64_t *offsets, const float *q, const float *qd,
+                               const float *u, float *dqdd, float *qdd, float *minv, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    std::vector<frg_traj> trajs;
+    if (!frg_offsets_to_trajs(n_traj, offsets, q, qd, u, dqdd, qdd, minv, trajs)) {
+        frg_set_error(ctx, "frg_gradient_ragged: offsets must be n_traj+1 non-decreasing values from 0, arrays non-null");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    return frg_gradient_batched(ctx, n_traj, trajs.data(), stream);
+}
+
+void *frg_host_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void frg_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"
+
+bool frg_offsets_to_trajs(int n_traj, const int64_t *offsets, const float *q, const float *qd, const float *u,
+                          float *dqdd, float *qdd, float *minv, std::vector<frg_traj> &out) {
+    if (n_traj < 0 || (n_traj > 0 && !offsets)) return false;
+    if (n_traj > 0 && offsets[0] != 0) return false;
+    for (int t = 0; t < n_traj; t++)
+        if (offsets[t + 1] < offsets[t]) return false;
+    const int64_t total = n_traj > 0 ? offsets[n_traj] : 0;
+    if (total > 0 && !(q && qd && u && dqdd && qdd && minv)) return false;
+    out.resize(static_cast<size_t>(n_traj));
+    for (int t = 0; t < n_traj; t++) {
+        const int64_t o = offsets[t];
+        out[t] = frg_traj{offsets[t + 1] - o, q + 7 * o, qd + 7 * o, u + 7 * o, dqdd + 98 * o, qdd + 7 * o,
+                          minv + 49 * o};
+    }
+    return true;
+}

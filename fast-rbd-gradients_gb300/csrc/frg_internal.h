@@ -1,0 +1,77 @@
+// Host-side internals shared by the C ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "frg.h"
+#include "frg_kernels.cuh"
+
+// Makes `device` current for a scope and restores the caller's device.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != device) cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// Descriptor list of a batched launch, built on the host.
+struct HostBatch {
+    std::vector<frg::Segment> segs;  // n_traj + 1 (end sentinel)
+    std::vector<int> tile_seg;       // one per 32-knot tile
+    long long nknots = 0;
+};
+
+// The same list on the device, plus the persistent kernel's work counter.
+struct DeviceBatch {
+    frg::Segment *segs = nullptr;
+    int *tile_seg = nullptr;
+    unsigned int *counter = nullptr;
+    int seg_cap = 0, tile_cap = 0;
+    bool reserve(int nseg_total, int ntiles_cap, std::string &err);
+    void release();
+};
+
+struct frg_ctx {
+    int device = 0;
+    bool damping = false, mpc = false;
+    frg::LaunchShape shape;
+    int num_sms = 0;
+    std::string err;
+    cudaStream_t io_stream = nullptr;   // frg_gradient_host
+    float *host_buf = nullptr;          // device staging for frg_gradient_host
+    size_t host_buf_floats = 0;
+    DeviceBatch scratch;                // frg_gradient_batched descriptors
+    cudaEvent_t scratch_done = nullptr;  // last launch that read `scratch`
+};
+
+struct frg_plan {
+    frg_ctx *ctx = nullptr;
+    DeviceBatch dev;
+    int nseg = 0, ntiles = 0;
+    long long nknots = 0;
+    cudaGraphExec_t exec = nullptr;
+};
+
+void frg_set_error(frg_ctx *ctx, const std::string &msg);
+bool frg_build_batch(int n_traj, const frg_traj *trajs, HostBatch &hb, std::string &err);
+cudaError_t frg_launch_batch(frg_ctx *ctx, const DeviceBatch &db, int nseg, int ntiles, cudaStream_t stream);
+bool frg_offsets_to_trajs(int n_traj, const int64_t *offsets, const float *q, const float *qd, const float *u,
+                          float *dqdd, float *qdd, float *minv, std::vector<frg_traj> &out);
+
+namespace frg {
+// Launch shape used until the autotuner or the caller picks one.
+inline LaunchShape default_shape() {
+    LaunchShape s;
+    s.warps_per_cta = 3;
+    s.ctas_per_sm = 3;
+    return s;
+}
+}  // namespace frg

@@ -1,0 +1,152 @@
+// sm_103a kernels for the iiwa_14 forward-dynamics gradient.
+//
+// Replaces the reference's dynamicsGradientKernel (helpers_GPU/
+// dynamicsGradient.cuh:1259-1290: one knot per 224-thread CTA, ~50 block
+// barriers per knot, q̈ and Minv computed on the host) with one knot per lane,
+// q̈ and Minv computed on the device, and no block barrier at all.
+#include "frg_kernels.cuh"
+#include "frg_knot.cuh"
+
+namespace frg {
+
+namespace {
+
+constexpr int kMaxWarpsPerCta = 8;
+
+struct PlainArgs {
+    const float *q, *qd, *u;
+    float *dqdd, *qdd, *minv;
+    int n;
+};
+
+__device__ __forceinline__ KnotPtrs plain_knot(const PlainArgs &a, int tile, int lane) {
+    const long long g = static_cast<long long>(tile) * 32 + lane;
+    if (g >= a.n) return KnotPtrs{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return KnotPtrs{a.q + 7 * g, a.qd + 7 * g, a.u + 7 * g, a.dqdd + 98 * g, a.qdd + 7 * g, a.minv + 49 * g};
+}
+
+template <bool DAMP, bool MPC>
+__global__ void __launch_bounds__(kMaxWarpsPerCta * 32) grad_plain_kernel(PlainArgs a) {
+    extern __shared__ float4 smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    const int warps_per_cta = blockDim.x >> 5;
+    const int ntiles = (a.n + 31) / 32;
+    for (int tile = blockIdx.x * warps_per_cta + warp; tile < ntiles; tile += gridDim.x * warps_per_cta) {
+        const KnotPtrs kp = plain_knot(a, tile, lane);
+        process_tile<DAMP, MPC>(ws, lane, kp);
+    }
+}
+
+__device__ __forceinline__ KnotPtrs ragged_knot(const Segment *segs, int nseg, const int *tile_seg, int tile,
+                                                int lane) {
+    const long long g = static_cast<long long>(tile) * 32 + lane;
+    if (g >= segs[nseg].knot_begin) return KnotPtrs{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int s = tile_seg[tile];
+    while (s + 1 < nseg && segs[s + 1].knot_begin <= g) s++;
+    const Segment &sg = segs[s];
+    const long long i = g - sg.knot_begin;
+    return KnotPtrs{sg.q + 7 * i, sg.qd + 7 * i, sg.u + 7 * i, sg.dqdd + 98 * i, sg.qdd + 7 * i, sg.minv + 49 * i};
+}
+
+// Persistent: each warp takes 32-knot tiles from a device work counter until
+// the list is exhausted.  The warp that draws the very last ticket
+// (ntiles + total_warps - 1: every warp fails exactly once) resets the counter,
+// so back-to-back and graph-replayed launches need no memset.
+template <bool DAMP, bool MPC>
+__global__ void __launch_bounds__(kMaxWarpsPerCta * 32)
+    grad_ragged_kernel(const Segment *segs, int nseg, const int *tile_seg, int ntiles, unsigned int *counter) {
+    extern __shared__ float4 smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    const unsigned int total_warps = gridDim.x * (blockDim.x >> 5);
+    for (;;) {
+        unsigned int ticket = 0;
+        if (lane == 0) ticket = atomicAdd(counter, 1u);
+        ticket = __shfl_sync(0xffffffffu, ticket, 0);
+        if (ticket >= static_cast<unsigned int>(ntiles)) {
+            if (lane == 0 && ticket == static_cast<unsigned int>(ntiles) + total_warps - 1u) atomicExch(counter, 0u);
+            return;
+        }
+        const KnotPtrs kp = ragged_knot(segs, nseg, tile_seg, static_cast<int>(ticket), lane);
+        process_tile<DAMP, MPC>(ws, lane, kp);
+    }
+}
+
+template <typename K>
+cudaError_t prepare(K kernel) {
+    static_assert(sizeof(WarpSmem) % 16 == 0, "warp smem must keep float4 alignment");
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(sizeof(WarpSmem)) * kMaxWarpsPerCta);
+}
+
+template <bool D, bool M>
+cudaError_t plain_impl(const LaunchShape &sh, const PlainArgs &a, cudaStream_t st) {
+    const int warps = sh.warps_per_cta;
+    const int ntiles = (a.n + 31) / 32;
+    const int grid = (ntiles + warps - 1) / warps;
+    grad_plain_kernel<D, M><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <bool D, bool M>
+cudaError_t ragged_impl(const LaunchShape &sh, int num_sms, const Segment *segs, int nseg, const int *tile_seg,
+                        int ntiles, unsigned int *counter, cudaStream_t st) {
+    const int warps = sh.warps_per_cta;
+    int grid = num_sms * sh.ctas_per_sm;
+    const int needed = (ntiles + warps - 1) / warps;
+    if (grid > needed) grid = needed;
+    if (grid < 1) grid = 1;
+    grad_ragged_kernel<D, M><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(segs, nseg, tile_seg, ntiles,
+                                                                                  counter);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t warp_smem_bytes() { return sizeof(WarpSmem); }
+
+cudaError_t init_kernels() {
+    cudaError_t e = cudaSuccess;
+    for (cudaError_t r : {prepare(grad_plain_kernel<false, false>), prepare(grad_plain_kernel<true, false>),
+                          prepare(grad_plain_kernel<false, true>), prepare(grad_plain_kernel<true, true>),
+                          prepare(grad_ragged_kernel<false, false>), prepare(grad_ragged_kernel<true, false>),
+                          prepare(grad_ragged_kernel<false, true>), prepare(grad_ragged_kernel<true, true>)})
+        if (r != cudaSuccess && e == cudaSuccess) e = r;
+    return e;
+}
+int max_warps_per_cta() { return kMaxWarpsPerCta; }
+
+int max_ctas_per_sm(int warps) {
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, grad_ragged_kernel<false, false>, warps * 32,
+                                                      sizeof(WarpSmem) * warps) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return blocks;
+}
+
+cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
+                         const float *u, float *dqdd, float *qdd, float *minv, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    if (shape.warps_per_cta < 1 || shape.warps_per_cta > kMaxWarpsPerCta) return cudaErrorInvalidValue;
+    const PlainArgs a{q, qd, u, dqdd, qdd, minv, n};
+    if (!damping && !mpc) return plain_impl<false, false>(shape, a, stream);
+    if (damping && !mpc) return plain_impl<true, false>(shape, a, stream);
+    if (!damping && mpc) return plain_impl<false, true>(shape, a, stream);
+    return plain_impl<true, true>(shape, a, stream);
+}
+
+cudaError_t launch_ragged(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const Segment *segs,
+                          int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream) {
+    if (ntiles <= 0) return cudaSuccess;
+    if (shape.warps_per_cta < 1 || shape.warps_per_cta > kMaxWarpsPerCta || shape.ctas_per_sm < 1)
+        return cudaErrorInvalidValue;
+    if (!damping && !mpc) return ragged_impl<false, false>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
+    if (damping && !mpc) return ragged_impl<true, false>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
+    if (!damping && mpc) return ragged_impl<false, true>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
+    return ragged_impl<true, true>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
+}
+
+}  // namespace frg

@@ -1,0 +1,44 @@
+// Kernel launch interface shared by the C ABI and the server (host side).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace frg {
+
+// One trajectory (or any contiguous run of knots) of a ragged batch.  Inputs
+// q/qd/u are [n][7], outputs dqdd [n][98], qdd [n][7], minv [n][49]; knot k
+// of the batch is segment s's knot (k - knot_begin).
+struct Segment {
+    const float *q, *qd, *u;
+    float *dqdd, *qdd, *minv;
+    long long knot_begin;
+};
+
+// Launch shape: warps per CTA (each warp owns 32 knots at a time) and, for the
+// persistent kernel, resident CTAs per SM.
+struct LaunchShape {
+    int warps_per_cta = 2;
+    int ctas_per_sm = 4;
+};
+
+size_t warp_smem_bytes();
+// Opt every kernel variant into the dynamic shared memory it needs (call once
+// per device, with that device current).
+cudaError_t init_kernels();
+int max_warps_per_cta();
+// Resident CTAs per SM of the batched kernel at `warps` warps per CTA.
+int max_ctas_per_sm(int warps);
+
+// Plain path: n knots, contiguous arrays, grid over 32-knot tiles.
+cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
+                         const float *u, float *dqdd, float *qdd, float *minv, cudaStream_t stream);
+
+// Ragged batch: one persistent launch walking 32-knot tiles of the
+// concatenated knot list.  segs[nseg + 1] (last = end sentinel with
+// knot_begin = total knots), tile_seg[ntiles] = segment of each tile's first
+// knot, counter = one device word, zero before the first launch (the kernel
+// leaves it zero again).
+cudaError_t launch_ragged(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const Segment *segs,
+                          int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream);
+
+}  // namespace frg

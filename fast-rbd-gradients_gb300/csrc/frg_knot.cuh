@@ -1,0 +1,528 @@
+// Per-knot forward-dynamics gradient, one knot per lane.
+//
+// Every lane of a warp carries one knot through the whole path, so the
+// inherently serial joint sweeps run without any block barrier, and all 32
+// lanes do useful work in every phase.  Lanes only meet at the per-warp
+// staging buffer that turns the knot-major HBM layout into coalesced 128-byte
+// loads and stores (__syncwarp only).
+//
+// Path per knot (the reference's forwardDynamicsGradientThreaded with
+// QDD_MINV_PASSED_IN=false, helpers_CPU/dynamicsGradient.h:869-934):
+//   1. sincos(q), RNEA with qdd = 0 -> bias = u - c (- 0.5 qd)     (:876-885)
+//   2. articulated-inertia sweep + Minv column passes            (minv.h:392-477)
+//   3. qdd = Minv bias, RNEA again with qdd                        (:892-895)
+//   4. d tau/dq, d tau/dqd as 13 independent tangent sweeps        (:787-857)
+//   5. dqdd = -Minv [d tau/dq | d tau/dqd]                         (:933)
+#pragma once
+#include "frg_model.cuh"
+
+namespace frg {
+
+// Per-link data that the tangent sweeps re-read, as float4 slots:
+//   0: v[0..3]   1: v[4..5] Iv[0..1]   2: Iv[2..5]   3: (X a_{k-1})[0,1,3,4]
+//   4: f_k[0,1,3,4] after the backward pass
+constexpr int kSlotsPerLink = 5;
+constexpr int kLinkSlots = kSlotsPerLink * kJoints;
+constexpr int kStageFloats = 49;  // per lane
+
+struct WarpSmem {
+    float4 link[kLinkSlots][32];
+    float stage[32 * kStageFloats];
+};
+
+// A lane's knot: input and output bases (q == nullptr: idle lane).
+struct KnotPtrs {
+    const float *q, *qd, *u;
+    float *dqdd, *qdd, *minv;
+};
+
+__device__ __forceinline__ const float *shfl_ptr(const float *p, int src) {
+    return reinterpret_cast<const float *>(
+        __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), src));
+}
+__device__ __forceinline__ float *shfl_ptr(float *p, int src) {
+    return reinterpret_cast<float *>(__shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), src));
+}
+
+// Coalesced gather of W floats per knot (knot-major) into stage[lane*W + j].
+template <int W>
+__device__ __forceinline__ void gather_in(float *stage, const float *base, int lane) {
+#pragma unroll
+    for (int e = lane; e < 32 * W; e += 32) {
+        const int kn = e / W, j = e - kn * W;
+        const float *p = shfl_ptr(base, kn);
+        stage[e] = p ? __ldg(p + j) : 0.0f;
+    }
+}
+
+// Coalesced scatter of stage[lane*W + j] to each knot's W floats at base.
+template <int W>
+__device__ __forceinline__ void scatter_out(const float *stage, float *base, int lane) {
+    __syncwarp();
+#pragma unroll 7
+    for (int e = lane; e < 32 * W; e += 32) {
+        const int kn = e / W, j = e - kn * W;
+        float *p = shfl_ptr(base, kn);
+        if (p) p[j] = stage[e];
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ void lds_link(const WarpSmem *ws, int k, int lane, float v[6], float Iv[6]) {
+    const float4 a = ws->link[kSlotsPerLink * k + 0][lane];
+    const float4 b = ws->link[kSlotsPerLink * k + 1][lane];
+    const float4 c = ws->link[kSlotsPerLink * k + 2][lane];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y;
+    Iv[0] = b.z; Iv[1] = b.w; Iv[2] = c.x; Iv[3] = c.y; Iv[4] = c.z; Iv[5] = c.w;
+}
+__device__ __forceinline__ void sts_link(WarpSmem *ws, int k, int lane, const float v[6], const float Iv[6]) {
+    ws->link[kSlotsPerLink * k + 0][lane] = make_float4(v[0], v[1], v[2], v[3]);
+    ws->link[kSlotsPerLink * k + 1][lane] = make_float4(v[4], v[5], Iv[0], Iv[1]);
+    ws->link[kSlotsPerLink * k + 2][lane] = make_float4(Iv[2], Iv[3], Iv[4], Iv[5]);
+}
+
+// ------------------------------------------------ articulated inertia ------
+
+// G = Rz N Rz^T for symmetric N (upper entries used), result symmetric.
+__device__ __forceinline__ void rotz_sym(float G[3][3], const float N[3][3], float c, float s) {
+    const float cc = c * c, ss = s * s, cs = c * s, d = cc - ss;
+    G[0][0] = fmaf(cc, N[0][0], fmaf(ss, N[1][1], -2.0f * cs * N[0][1]));
+    G[1][1] = fmaf(ss, N[0][0], fmaf(cc, N[1][1], 2.0f * cs * N[0][1]));
+    G[0][1] = fmaf(cs, N[0][0] - N[1][1], d * N[0][1]);
+    G[0][2] = fmaf(c, N[0][2], -s * N[1][2]);
+    G[1][2] = fmaf(s, N[0][2], c * N[1][2]);
+    G[2][2] = N[2][2];
+    G[1][0] = G[0][1]; G[2][0] = G[0][2]; G[2][1] = G[1][2];
+}
+
+// G = Rz N Rz^T for general N.
+__device__ __forceinline__ void rotz_gen(float G[3][3], const float N[3][3], float c, float s) {
+    float H[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        H[0][j] = fmaf(c, N[0][j], -s * N[1][j]);
+        H[1][j] = fmaf(s, N[0][j], c * N[1][j]);
+        H[2][j] = N[2][j];
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        G[i][0] = fmaf(c, H[i][0], -s * H[i][1]);
+        G[i][1] = fmaf(s, H[i][0], c * H[i][1]);
+        G[i][2] = H[i][2];
+    }
+}
+
+// O = F^T G F:  O[i][j] = s_i s_j G[p_i][p_j]
+template <int k> __device__ __forceinline__ void perm_FT_G_F(float O[3][3], const float G[3][3]) {
+    using J = Joint<k>;
+    constexpr int p[3] = {J::p0, J::p1, J::p2};
+    constexpr float sg[3] = {J::s0, J::s1, J::s2};
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) O[i][j] = (sg[i] * sg[j]) * G[p[i]][p[j]];
+}
+
+// X_k^T [A B; B^T M] X_k for the joint transform X_k = [E 0; -E r^ E].
+// With At = E^T A E, Bt = E^T B E, Mt = E^T M E:
+//   M' = Mt,  B' = Bt + r^ Mt,  A' = At + r^ Bt^T - B' r^.
+template <int k>
+__device__ __forceinline__ void congruence(float Ao[3][3], float Bo[3][3], float Mo[3][3], const float A[3][3],
+                                           const float B[3][3], const float M[3][3], float c, float s) {
+    using J = Joint<k>;
+    float G[3][3], At[3][3], Bt[3][3];
+    rotz_sym(G, A, c, s);
+    perm_FT_G_F<k>(At, G);
+    rotz_gen(G, B, c, s);
+    perm_FT_G_F<k>(Bt, G);
+    rotz_sym(G, M, c, s);
+    perm_FT_G_F<k>(Mo, G);
+    const float t = J::t;
+    if constexpr (J::axis == 2) {
+        // r^ = [0 -t 0; t 0 0; 0 0 0]
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            Bo[0][j] = fmaf(-t, Mo[1][j], Bt[0][j]);
+            Bo[1][j] = fmaf(t, Mo[0][j], Bt[1][j]);
+            Bo[2][j] = Bt[2][j];
+        }
+        // (r^ Bt^T)[i][j]: i=0: -t Bt[j][1]; i=1: t Bt[j][0]; i=2: 0
+        // (B' r^)[i][j]:   j=0: t B'[i][1]; j=1: -t B'[i][0]; j=2: 0
+        Ao[0][0] = fmaf(-t, Bt[0][1], fmaf(-t, Bo[0][1], At[0][0]));
+        Ao[0][1] = fmaf(-t, Bt[1][1], fmaf(t, Bo[0][0], At[0][1]));
+        Ao[0][2] = fmaf(-t, Bt[2][1], At[0][2]);
+        Ao[1][1] = fmaf(t, Bt[1][0], fmaf(t, Bo[1][0], At[1][1]));
+        Ao[1][2] = fmaf(t, Bt[2][0], At[1][2]);
+        Ao[2][2] = At[2][2];
+    } else {
+        // r^ = [0 0 t; 0 0 0; -t 0 0]
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            Bo[0][j] = fmaf(t, Mo[2][j], Bt[0][j]);
+            Bo[1][j] = Bt[1][j];
+            Bo[2][j] = fmaf(-t, Mo[0][j], Bt[2][j]);
+        }
+        // (r^ Bt^T)[i][j]: i=0: t Bt[j][2]; i=1: 0; i=2: -t Bt[j][0]
+        // (B' r^)[i][j]:   j=0: -t B'[i][2]; j=1: 0; j=2: t B'[i][0]
+        Ao[0][0] = fmaf(t, Bt[0][2], fmaf(t, Bo[0][2], At[0][0]));
+        Ao[0][1] = fmaf(t, Bt[1][2], At[0][1]);
+        Ao[0][2] = fmaf(t, Bt[2][2], fmaf(-t, Bo[0][0], At[0][2]));
+        Ao[1][1] = At[1][1];
+        Ao[1][2] = fmaf(-t, Bo[1][0], At[1][2]);
+        Ao[2][2] = fmaf(-t, Bt[2][0], fmaf(-t, Bo[2][0], At[2][2]));
+    }
+    Ao[1][0] = Ao[0][1]; Ao[2][0] = Ao[0][2]; Ao[2][1] = Ao[1][2];
+}
+
+// IA_k = I_k + child carry, as blocks [A B; B^T M].
+template <int k>
+__device__ __forceinline__ void add_link_inertia(float A[3][3], float B[3][3], float M[3][3]) {
+    using L = Link<k>;
+    A[0][0] += L::Ixx; A[1][1] += L::Iyy; A[2][2] += L::Izz;
+    A[0][1] += L::Ixy; A[1][0] += L::Ixy;
+    A[0][2] += L::Ixz; A[2][0] += L::Ixz;
+    A[1][2] += L::Iyz; A[2][1] += L::Iyz;
+    // m c^ = [0 -mcz mcy; mcz 0 -mcx; -mcy mcx 0]
+    B[0][1] += -L::mcz; B[0][2] += L::mcy;
+    B[1][0] += L::mcz;  B[1][2] += -L::mcx;
+    B[2][0] += -L::mcy; B[2][1] += L::mcx;
+    M[0][0] += L::m; M[1][1] += L::m; M[2][2] += L::m;
+}
+
+// ------------------------------------------------------------- phase 1 -----
+
+// sincos, RNEA(q, qd, 0), bias, Minv (upper triangle, Mi[i][j] for i <= j), qdd.
+// Leaves v_k and I_k v_k of every link in the warp's link slots.
+template <bool DAMP, bool MPC>
+__device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7], const float qd[7], const float u[7],
+                                       float sq[7], float cq[7], float Mi[7][7], float qdd[7]) {
+#pragma unroll
+    for (int k = 0; k < kJoints; k++) sincosf(q[k], &sq[k], &cq[k]);
+
+    // RNEA forward with qdd = 0 (RNEA_fp, dynamicsGradient.h:620-659)
+    float f[kJoints][6];
+    {
+        float v[6], a[6];
+        static_for<0, kJoints>([&](auto K) {
+            constexpr int k = decltype(K)::value;
+            if constexpr (k == 0) {
+                v[0] = v[1] = 0.0f; v[2] = qd[0]; v[3] = v[4] = v[5] = 0.0f;
+                if constexpr (MPC) {
+#pragma unroll
+                    for (int i = 0; i < 6; i++) a[i] = 0.0f;
+                } else {
+                    const float g[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, kGravity};
+                    xmotion<0>(a, g, cq[0], sq[0]);
+                }
+            } else {
+                float nv[6], na[6];
+                xmotion<k>(nv, v, cq[k], sq[k]);
+                nv[2] += qd[k];
+                xmotion<k>(na, a, cq[k], sq[k]);
+                na[0] = fmaf(nv[1], qd[k], na[0]);
+                na[1] = fmaf(-nv[0], qd[k], na[1]);
+                na[3] = fmaf(nv[4], qd[k], na[3]);
+                na[4] = fmaf(-nv[3], qd[k], na[4]);
+#pragma unroll
+                for (int i = 0; i < 6; i++) { v[i] = nv[i]; a[i] = na[i]; }
+            }
+            float Iv[6];
+            imul<k>(Iv, v);
+            imul<k>(f[k], a);
+            crf_acc(f[k], v, Iv);
+            sts_link(ws, k, lane, v, Iv);
+        });
+    }
+    // backward (RNEA_bp :662-670) -> c, bias (computeBias :677-683)
+    float bias[kJoints];
+    static_for_down<kJoints - 1, 0>([&](auto K) {
+        constexpr int k = decltype(K)::value;
+        const float c = f[k][2];
+        bias[k] = DAMP ? u[k] - fmaf(0.5f, qd[k], c) : u[k] - c;
+        if constexpr (k > 0) {
+            float t[6];
+            xforce_T<k>(t, f[k], cq[k], sq[k]);
+#pragma unroll
+            for (int i = 0; i < 6; i++) f[k - 1][i] += t[i];
+        }
+    });
+
+    // articulated-inertia sweep: U_k = IA_k[:,2], D_k = U_k[2]
+    // (Minv_bp :424-436; compute_Ia_revolute :147; ctransform_Ia_revolute :222)
+    float U[kJoints][6], Dinv[kJoints];
+    {
+        float A[3][3], B[3][3], M[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) A[i][j] = B[i][j] = M[i][j] = 0.0f;
+        static_for_down<kJoints - 1, 0>([&](auto K) {
+            constexpr int k = decltype(K)::value;
+            add_link_inertia<k>(A, B, M);
+            U[k][0] = A[0][2]; U[k][1] = A[1][2]; U[k][2] = A[2][2];
+            U[k][3] = B[2][0]; U[k][4] = B[2][1]; U[k][5] = B[2][2];
+            Dinv[k] = 1.0f / U[k][2];
+            if constexpr (k > 0) {
+                // Ia = IA - U U^T / D with the joint row/column exactly zero
+                float Ud[6];
+#pragma unroll
+                for (int i = 0; i < 6; i++) Ud[i] = U[k][i] * Dinv[k];
+                float Aa[3][3], Ba[3][3], Ma[3][3];
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        Aa[i][j] = (i == 2 || j == 2) ? 0.0f : fmaf(-U[k][i], Ud[j], A[i][j]);
+                        Ba[i][j] = (i == 2) ? 0.0f : fmaf(-U[k][i], Ud[3 + j], B[i][j]);
+                        Ma[i][j] = fmaf(-U[k][3 + i], Ud[3 + j], M[i][j]);
+                    }
+                congruence<k>(A, B, M, Aa, Ba, Ma, cq[k], sq[k]);
+            }
+        });
+    }
+
+    // Minv columns: backward pass (bwdPassMinvFUpdate, minv.h:392-412) then
+    // forward pass (fwdPassUpdate, :440-461), each column carrying one F vector.
+    static_for<0, kJoints>([&](auto JJ) {
+        constexpr int j = decltype(JJ)::value;
+        float F[6];
+        static_for_down<j, 0>([&](auto II) {
+            constexpr int i = decltype(II)::value;
+            if constexpr (i == j) {
+                Mi[j][j] = Dinv[j];
+#pragma unroll
+                for (int r = 0; r < 6; r++) F[r] = U[j][r] * Dinv[j];
+            } else {
+                const float m = -Dinv[i] * F[2];
+                Mi[i][j] = m;
+#pragma unroll
+                for (int r = 0; r < 6; r++) F[r] = fmaf(U[i][r], m, F[r]);
+            }
+            if constexpr (i > 0) {
+                float t[6];
+                xforce_T<i>(t, F, cq[i], sq[i]);
+#pragma unroll
+                for (int r = 0; r < 6; r++) F[r] = t[r];
+            }
+        });
+        static_for<0, j + 1>([&](auto II) {
+            constexpr int i = decltype(II)::value;
+            if constexpr (i == 0) {
+#pragma unroll
+                for (int r = 0; r < 6; r++) F[r] = 0.0f;
+                F[2] = Mi[0][j];
+            } else {
+                // Minv[i][j] -= D_i^-1 U_i^T X_i F_{i-1};  F_i = S Minv[i][j] + X_i F_{i-1}
+                float y[6];
+                xmotion<i>(y, F, cq[i], sq[i]);
+                float d = U[i][0] * y[0];
+#pragma unroll
+                for (int r = 1; r < 6; r++) d = fmaf(U[i][r], y[r], d);
+                Mi[i][j] = fmaf(-Dinv[i], d, Mi[i][j]);
+#pragma unroll
+                for (int r = 0; r < 6; r++) F[r] = y[r];
+                F[2] += Mi[i][j];
+            }
+        });
+    });
+
+    // qdd = Minv_sym bias (matVMultSym, math.h:29-37)
+#pragma unroll
+    for (int r = 0; r < kJoints; r++) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kJoints; k++) acc = fmaf(r <= k ? Mi[r][k] : Mi[k][r], bias[k], acc);
+        qdd[r] = acc;
+    }
+}
+
+// RNEA(q, qd, qdd) forward + backward: stores (X_k a_{k-1})[0,1,3,4] and the
+// accumulated f_k[0,1,3,4] in the link slots (read at the diagonal step of the
+// d/dq sweeps).
+template <bool MPC>
+__device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const float qd[7], const float qdd[7],
+                                              const float sq[7], const float cq[7]) {
+    float f[kJoints][6];
+    float a[6];
+    static_for<0, kJoints>([&](auto K) {
+        constexpr int k = decltype(K)::value;
+        float v[6], Iv[6];
+        lds_link(ws, k, lane, v, Iv);
+        if constexpr (k == 0) {
+            if constexpr (MPC) {
+#pragma unroll
+                for (int i = 0; i < 6; i++) a[i] = 0.0f;
+            } else {
+                const float g[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, kGravity};
+                xmotion<0>(a, g, cq[0], sq[0]);
+            }
+            a[2] += qdd[0];
+        } else {
+            float xa[6];
+            xmotion<k>(xa, a, cq[k], sq[k]);
+            ws->link[kSlotsPerLink * k + 3][lane] = make_float4(xa[0], xa[1], xa[3], xa[4]);
+            a[0] = fmaf(v[1], qd[k], xa[0]);
+            a[1] = fmaf(-v[0], qd[k], xa[1]);
+            a[2] = xa[2] + qdd[k];
+            a[3] = fmaf(v[4], qd[k], xa[3]);
+            a[4] = fmaf(-v[3], qd[k], xa[4]);
+            a[5] = xa[5];
+        }
+        imul<k>(f[k], a);
+        crf_acc(f[k], v, Iv);
+    });
+    static_for_down<kJoints - 1, 1>([&](auto K) {
+        constexpr int k = decltype(K)::value;
+        ws->link[kSlotsPerLink * k + 4][lane] = make_float4(f[k][0], f[k][1], f[k][3], f[k][4]);
+        float t[6];
+        xforce_T<k>(t, f[k], cq[k], sq[k]);
+#pragma unroll
+        for (int i = 0; i < 6; i++) f[k - 1][i] += t[i];
+    });
+}
+
+// ------------------------------------------------------------- phase 2 -----
+
+// One column of d tau / dq (QSIDE) or d tau / dqd for the differentiated joint c
+// (compute_vafdu :787-829 and compute_cdu :832-857 restricted to column c).
+template <bool QSIDE, bool DAMP>
+__device__ __forceinline__ void dtau_column(const WarpSmem *ws, int lane, int c, const float qd[7],
+                                            const float sq[7], const float cq[7], float dtau[7]) {
+    float df[kJoints][6];
+    float dv[6], da[6];
+    static_for<0, kJoints>([&](auto K) {
+        constexpr int k = decltype(K)::value;
+        if (k >= c) {
+            float v[6], Iv[6];
+            lds_link(ws, k, lane, v, Iv);
+            float ndv[6], nda[6], Idv[6];
+            if (k == c) {
+                if constexpr (QSIDE) {
+                    // dv = crm(X_k v_{k-1}) S; (X_k v_{k-1}) and v_k agree outside entry 2
+                    ndv[0] = v[1]; ndv[1] = -v[0]; ndv[2] = 0.0f;
+                    ndv[3] = v[4]; ndv[4] = -v[3]; ndv[5] = 0.0f;
+                    // da = crm(dv) S qd_k + crm(X_k a_{k-1}) S
+                    const float4 xa = ws->link[kSlotsPerLink * k + 3][lane];  // (Xa0, Xa1, Xa3, Xa4)
+                    nda[0] = fmaf(ndv[1], qd[k], xa.y);
+                    nda[1] = fmaf(-ndv[0], qd[k], -xa.x);
+                    nda[2] = 0.0f;
+                    nda[3] = fmaf(ndv[4], qd[k], xa.w);
+                    nda[4] = fmaf(-ndv[3], qd[k], -xa.z);
+                    nda[5] = 0.0f;
+                    imul<k>(Idv, ndv);
+                } else {
+                    // dv = S, da = crm(v_k) S, I dv = I_k[:,2]
+                    ndv[0] = ndv[1] = 0.0f; ndv[2] = 1.0f; ndv[3] = ndv[4] = ndv[5] = 0.0f;
+                    nda[0] = v[1]; nda[1] = -v[0]; nda[2] = 0.0f;
+                    nda[3] = v[4]; nda[4] = -v[3]; nda[5] = 0.0f;
+                    icol2<k>(Idv);
+                }
+            } else {
+                xmotion<k>(ndv, dv, cq[k], sq[k]);
+                xmotion<k>(nda, da, cq[k], sq[k]);
+                nda[0] = fmaf(ndv[1], qd[k], nda[0]);
+                nda[1] = fmaf(-ndv[0], qd[k], nda[1]);
+                nda[3] = fmaf(ndv[4], qd[k], nda[3]);
+                nda[4] = fmaf(-ndv[3], qd[k], nda[4]);
+                imul<k>(Idv, ndv);
+            }
+            // df = I da + dv x* (I v) + v x* (I dv)
+            imul<k>(df[k], nda);
+            crf_acc(df[k], ndv, Iv);
+            crf_acc(df[k], v, Idv);
+#pragma unroll
+            for (int i = 0; i < 6; i++) { dv[i] = ndv[i]; da[i] = nda[i]; }
+        }
+    });
+    float dF[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    static_for_down<kJoints - 1, 0>([&](auto K) {
+        constexpr int k = decltype(K)::value;
+        if (k >= c) {
+#pragma unroll
+            for (int i = 0; i < 6; i++) dF[i] += df[k][i];
+        }
+        dtau[k] = dF[2];
+        if constexpr (k > 0) {
+            if (QSIDE && k == c) {
+                // + X_k^T (S x* f_k)
+                const float4 fs = ws->link[kSlotsPerLink * k + 4][lane];  // (f0, f1, f3, f4)
+                dF[0] -= fs.y; dF[1] += fs.x; dF[3] -= fs.w; dF[4] += fs.z;
+            }
+            float t[6];
+            xforce_T<k>(t, dF, cq[k], sq[k]);
+#pragma unroll
+            for (int i = 0; i < 6; i++) dF[i] = t[i];
+        }
+    });
+    if (!QSIDE && DAMP) dtau[c] += 0.5f;
+}
+
+// out = -Minv_sym dtau
+__device__ __forceinline__ void minv_times(float out[7], const float Mi[7][7], const float dtau[7]) {
+#pragma unroll
+    for (int r = 0; r < kJoints; r++) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kJoints; k++) acc = fmaf(r <= k ? Mi[r][k] : Mi[k][r], dtau[k], acc);
+        out[r] = -acc;
+    }
+}
+
+// Full path for the 32 knots of one warp tile.
+template <bool DAMP, bool MPC>
+__device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotPtrs &kp) {
+    float q[7], qd[7], u[7];
+    gather_in<7>(ws->stage, kp.q, lane);
+    gather_in<7>(ws->stage + 224, kp.qd, lane);
+    gather_in<7>(ws->stage + 448, kp.u, lane);
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        q[j] = ws->stage[lane * 7 + j];
+        qd[j] = ws->stage[224 + lane * 7 + j];
+        u[j] = ws->stage[448 + lane * 7 + j];
+    }
+    __syncwarp();
+
+    float sq[7], cq[7], Mi[7][7], qdd[7];
+    phase1<DAMP, MPC>(ws, lane, q, qd, u, sq, cq, Mi, qdd);
+
+    // Minv (dense) and qdd out
+#pragma unroll
+    for (int c = 0; c < 7; c++)
+#pragma unroll
+        for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r + 7 * c] = r <= c ? Mi[r][c] : Mi[c][r];
+    scatter_out<49>(ws->stage, kp.minv, lane);
+#pragma unroll
+    for (int r = 0; r < 7; r++) ws->stage[lane * 7 + r] = qdd[r];
+    scatter_out<7>(ws->stage, kp.qdd, lane);
+
+    rnea_with_qdd<MPC>(ws, lane, qd, qdd, sq, cq);
+    __syncwarp();
+
+    // d qdd / dq: columns 0..6 (column 0 is identically zero for this model:
+    // the base joint axis is parallel to gravity, as dynamicsGradient.h:797-813 uses)
+#pragma unroll
+    for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r] = 0.0f;
+#pragma unroll 1
+    for (int c = 1; c < kJoints; c++) {
+        float dtau[7], out[7];
+        dtau_column<true, DAMP>(ws, lane, c, qd, sq, cq, dtau);
+        minv_times(out, Mi, dtau);
+#pragma unroll
+        for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
+    }
+    scatter_out<49>(ws->stage, kp.dqdd, lane);
+    // d qdd / dqd: columns 7..13
+#pragma unroll 1
+    for (int c = 0; c < kJoints; c++) {
+        float dtau[7], out[7];
+        dtau_column<false, DAMP>(ws, lane, c, qd, sq, cq, dtau);
+        minv_times(out, Mi, dtau);
+#pragma unroll
+        for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
+    }
+    scatter_out<49>(ws->stage, kp.dqdd ? kp.dqdd + 49 : nullptr, lane);
+}
+
+}  // namespace frg

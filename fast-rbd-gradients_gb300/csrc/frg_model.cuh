@@ -1,0 +1,200 @@
+// iiwa_14 model and spatial algebra for the sm_103a kernels.
+//
+// The reference code-generates the model as dense 6x6 constants
+// (helpers_CPU/dynamicsGradient.h:124-229, :231-587; helpers_GPU/
+// dynamicsGradient.cuh:313-407).  Here each joint transform is described by
+// its structure instead:
+//
+//   iX(i-1) = [E 0; -E r^ E],   E = Rz(q)^T F,
+//
+// F a fixed signed permutation (the joint frame's rpy from utils/iiwa_14.urdf)
+// and r = t * e_axis the joint origin (one nonzero component for every iiwa
+// joint).  Applying X or X^T then costs two plane rotations and two FMAs.  The
+// spatial inertias use the structure I = [Ibar, m c^; m c^T, m 1] with
+// compile-time constants, so structurally zero terms drop out at compile time.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace frg {
+
+constexpr int kJoints = 7;
+constexpr float kGravity = 9.81f;  // GRAVITY default, dynamicsGradient.h:7-9
+
+template <int N> struct IC { static constexpr int value = N; };
+
+// Compile-time loops (the link index must be a constant expression so that the
+// per-joint structure and the register arrays indexed by it resolve statically).
+template <int B, int E, typename F> __device__ __forceinline__ void static_for(F &&f) {
+    if constexpr (B < E) {
+        f(IC<B>{});
+        static_for<B + 1, E>(f);
+    }
+}
+template <int B, int E, typename F> __device__ __forceinline__ void static_for_down(F &&f) {
+    if constexpr (B >= E) {
+        f(IC<B>{});
+        static_for_down<B - 1, E>(f);
+    }
+}
+
+// ------------------------------------------------------------------ model ---
+
+// Link inertial data of utils/iiwa_14.urdf (iiwa_link_1..7): inertia at the
+// COM (xx xy xz yy yz zz), COM position (x y z), mass.  The same numbers as the
+// reference's l0..l6 constants (dynamicsGradient.h:127-202).
+struct LinkInertial { double ixx, ixy, ixz, iyy, iyz, izz, cx, cy, cz, m; };
+constexpr LinkInertial kLinks[kJoints] = {
+    {0.121, 0.0, 0.0, 0.116, -0.021, 0.0175, 0.0, -0.03, 0.12, 5.76},
+    {0.0638, 0.0001, 0.00008, 0.0416, 0.0157, 0.0331, 0.0003, 0.059, 0.042, 6.35},
+    {0.0873, 0.0, 0.0, 0.083, 0.014, 0.0108, 0.0, 0.03, 0.13, 3.5},
+    {0.0368, 0.0, 0.0, 0.02045, 0.008, 0.02171, 0.0, 0.067, 0.034, 3.5},
+    {0.0318, 0.000007, 0.000027, 0.028916, 0.005586, 0.006, 0.0001, 0.021, 0.076, 3.5},
+    {0.0049, 0.0, 0.0, 0.0047, 0.0, 0.0036, 0.0, 0.0006, 0.0004, 1.8},
+    {0.0055, 0.0, 0.0, 0.0055, 0.0, 0.005, 0.0, 0.0, 0.02, 1.2},
+};
+
+// Spatial inertia about the joint origin: rotational block Ibar = Icom +
+// m (|c|^2 1 - c c^T) (the parallel-axis shift buildI6x6 applies,
+// dynamicsGradient.h:78-118), coupling m c, mass m.
+template <int k> struct Link {
+    static constexpr LinkInertial L = kLinks[k];
+    static constexpr float Ixx = float(L.ixx + L.m * (L.cy * L.cy + L.cz * L.cz));
+    static constexpr float Iyy = float(L.iyy + L.m * (L.cx * L.cx + L.cz * L.cz));
+    static constexpr float Izz = float(L.izz + L.m * (L.cx * L.cx + L.cy * L.cy));
+    static constexpr float Ixy = float(L.ixy - L.m * L.cx * L.cy);
+    static constexpr float Ixz = float(L.ixz - L.m * L.cx * L.cz);
+    static constexpr float Iyz = float(L.iyz - L.m * L.cy * L.cz);
+    static constexpr float mcx = float(L.m * L.cx), mcy = float(L.m * L.cy), mcz = float(L.m * L.cz);
+    static constexpr float m = float(L.m);
+};
+
+// Joint frames (utils/iiwa_14.urdf iiwa_joint_1..7 <origin>).  F maps w to
+// (F w)[p_i] = s_i w_i; axis/t give r = t e_axis (axis 1 = y, 2 = z).
+//   rpy (0,0,0):                 p = {0,1,2}, s = {+,+,+}
+//   rpy (pi/2,0,pi), (-pi/2,pi,0): p = {0,2,1}, s = {-,+,+}   w -> (-w0, w2, w1)
+//   rpy (pi/2,0,0):              p = {0,2,1}, s = {+,-,+}   w -> (w0, w2, -w1)
+// Translations as tz_j1..ty_j7, dynamicsGradient.h:223-229.
+template <int k> struct Joint;
+template <> struct Joint<0> { static constexpr int p0 = 0, p1 = 1, p2 = 2; static constexpr float s0 = 1, s1 = 1, s2 = 1; static constexpr int axis = 2; static constexpr float t = 0.1575f; };
+template <> struct Joint<1> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 2; static constexpr float t = 0.2025f; };
+template <> struct Joint<2> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr float t = 0.2045f; };
+template <> struct Joint<3> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = 1, s1 = -1, s2 = 1; static constexpr int axis = 2; static constexpr float t = 0.2155f; };
+template <> struct Joint<4> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr float t = 0.1845f; };
+template <> struct Joint<5> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = 1, s1 = -1, s2 = 1; static constexpr int axis = 2; static constexpr float t = 0.2155f; };
+template <> struct Joint<6> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr float t = 0.081f; };
+
+// ------------------------------------------------------- 3-vector pieces ---
+
+// E w = Rz(q)^T (F w)
+template <int k> __device__ __forceinline__ void rot_E(float o[3], const float w[3], float c, float s) {
+    using J = Joint<k>;
+    float fw[3];
+    fw[J::p0] = J::s0 * w[0];
+    fw[J::p1] = J::s1 * w[1];
+    fw[J::p2] = J::s2 * w[2];
+    o[0] = fmaf(c, fw[0], s * fw[1]);
+    o[1] = fmaf(c, fw[1], -s * fw[0]);
+    o[2] = fw[2];
+}
+
+// E^T w = F^T (Rz(q) w),  (F^T x)_i = s_i x[p_i]
+template <int k> __device__ __forceinline__ void rot_ET(float o[3], const float w[3], float c, float s) {
+    using J = Joint<k>;
+    float x[3];
+    x[0] = fmaf(c, w[0], -s * w[1]);
+    x[1] = fmaf(c, w[1], s * w[0]);
+    x[2] = w[2];
+    o[0] = J::s0 * x[J::p0];
+    o[1] = J::s1 * x[J::p1];
+    o[2] = J::s2 * x[J::p2];
+}
+
+// o = u - r x w  (r = t e_axis)
+template <int k> __device__ __forceinline__ void sub_r_cross(float o[3], const float u[3], const float w[3]) {
+    using J = Joint<k>;
+    if constexpr (J::axis == 2) {  // r x w = (-t w1, t w0, 0)
+        o[0] = fmaf(J::t, w[1], u[0]);
+        o[1] = fmaf(-J::t, w[0], u[1]);
+        o[2] = u[2];
+    } else {  // axis y: r x w = (t w2, 0, -t w0)
+        o[0] = fmaf(-J::t, w[2], u[0]);
+        o[1] = u[1];
+        o[2] = fmaf(J::t, w[0], u[2]);
+    }
+}
+
+// o = u + r x w
+template <int k> __device__ __forceinline__ void add_r_cross(float o[3], const float u[3], const float w[3]) {
+    using J = Joint<k>;
+    if constexpr (J::axis == 2) {
+        o[0] = fmaf(-J::t, w[1], u[0]);
+        o[1] = fmaf(J::t, w[0], u[1]);
+        o[2] = u[2];
+    } else {
+        o[0] = fmaf(J::t, w[2], u[0]);
+        o[1] = u[1];
+        o[2] = fmaf(-J::t, w[0], u[2]);
+    }
+}
+
+// ------------------------------------------------------- spatial vectors ---
+
+// y = X_k x  (motion vector to the child frame):  [E w; E (v - r x w)]
+template <int k> __device__ __forceinline__ void xmotion(float y[6], const float x[6], float c, float s) {
+    float u[3];
+    rot_E<k>(y, x, c, s);
+    sub_r_cross<k>(u, x + 3, x);
+    rot_E<k>(y + 3, u, c, s);
+}
+
+// y = X_k^T x  (force vector to the parent frame):  [E^T n + r x (E^T f); E^T f]
+template <int k> __device__ __forceinline__ void xforce_T(float y[6], const float x[6], float c, float s) {
+    float n[3];
+    rot_ET<k>(y + 3, x + 3, c, s);
+    rot_ET<k>(n, x, c, s);
+    add_r_cross<k>(y, n, y + 3);
+}
+
+#define FRG_ACC(acc, K, x)                   \
+    if constexpr ((K) != 0.0f) {             \
+        acc = fmaf((K), (x), acc);           \
+    }
+
+// y = I_k w:  [Ibar w + mc x v; m v - mc x w]
+template <int k> __device__ __forceinline__ void imul(float y[6], const float x[6]) {
+    using L = Link<k>;
+    const float w0 = x[0], w1 = x[1], w2 = x[2], v0 = x[3], v1 = x[4], v2 = x[5];
+    float t0 = L::Ixx * w0, t1 = L::Iyy * w1, t2 = L::Izz * w2;
+    FRG_ACC(t0, L::Ixy, w1) FRG_ACC(t0, L::Ixz, w2)
+    FRG_ACC(t1, L::Ixy, w0) FRG_ACC(t1, L::Iyz, w2)
+    FRG_ACC(t2, L::Ixz, w0) FRG_ACC(t2, L::Iyz, w1)
+    // + mc x v = (mcy v2 - mcz v1, mcz v0 - mcx v2, mcx v1 - mcy v0)
+    FRG_ACC(t0, L::mcy, v2) FRG_ACC(t0, -L::mcz, v1)
+    FRG_ACC(t1, L::mcz, v0) FRG_ACC(t1, -L::mcx, v2)
+    FRG_ACC(t2, L::mcx, v1) FRG_ACC(t2, -L::mcy, v0)
+    float b0 = L::m * v0, b1 = L::m * v1, b2 = L::m * v2;
+    // - mc x w
+    FRG_ACC(b0, -L::mcy, w2) FRG_ACC(b0, L::mcz, w1)
+    FRG_ACC(b1, -L::mcz, w0) FRG_ACC(b1, L::mcx, w2)
+    FRG_ACC(b2, -L::mcx, w1) FRG_ACC(b2, L::mcy, w0)
+    y[0] = t0; y[1] = t1; y[2] = t2; y[3] = b0; y[4] = b1; y[5] = b2;
+}
+
+// y = I_k S = I_k e_2 (third column, constant)
+template <int k> __device__ __forceinline__ void icol2(float y[6]) {
+    using L = Link<k>;
+    y[0] = L::Ixz; y[1] = L::Iyz; y[2] = L::Izz;
+    y[3] = -L::mcy; y[4] = L::mcx; y[5] = 0.0f;
+}
+
+// y += crf(v) h = v x* h
+__device__ __forceinline__ void crf_acc(float y[6], const float v[6], const float h[6]) {
+    y[0] = fmaf(v[1], h[2], fmaf(-v[2], h[1], fmaf(v[4], h[5], fmaf(-v[5], h[4], y[0]))));
+    y[1] = fmaf(v[2], h[0], fmaf(-v[0], h[2], fmaf(v[5], h[3], fmaf(-v[3], h[5], y[1]))));
+    y[2] = fmaf(v[0], h[1], fmaf(-v[1], h[0], fmaf(v[3], h[4], fmaf(-v[4], h[3], y[2]))));
+    y[3] = fmaf(v[1], h[5], fmaf(-v[2], h[4], y[3]));
+    y[4] = fmaf(v[2], h[3], fmaf(-v[0], h[5], y[4]));
+    y[5] = fmaf(v[0], h[4], fmaf(-v[1], h[3], y[5]));
+}
+
+}  // namespace frg

@@ -1,0 +1,186 @@
+// Plans (batched launches prepared once and replayed as CUDA graphs) and the
+// launch-shape autotuner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <new>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "frg.h"
+#include "frg_internal.h"
+#include "frg_kernels.cuh"
+
+namespace {
+
+bool ok(frg_ctx *ctx, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return true;
+    frg_set_error(ctx, std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+// Captures one batched launch of `plan` into an executable graph.
+bool capture(frg_plan *plan) {
+    frg_ctx *ctx = plan->ctx;
+    cudaStream_t cs = nullptr;
+    if (!ok(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream")) return false;
+    bool good = ok(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    cudaGraph_t graph = nullptr;
+    if (good) {
+        cudaError_t le = frg_launch_batch(ctx, plan->dev, plan->nseg, plan->ntiles, cs);
+        cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+        good = ok(ctx, le, "batched launch capture") && ok(ctx, ee, "cudaStreamEndCapture");
+    }
+    if (good) good = ok(ctx, cudaGraphInstantiate(&plan->exec, graph, 0), "cudaGraphInstantiate");
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    return good;
+}
+
+}  // namespace
+
+extern "C" {
+
+frg_status frg_plan_create(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_plan **out) {
+    if (!ctx || !out) return FRG_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (n_traj < 0 || (n_traj > 0 && !trajs)) {
+        frg_set_error(ctx, "frg_plan_create: bad trajectory list");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    HostBatch hb;
+    std::string err;
+    if (!frg_build_batch(n_traj, trajs, hb, err)) {
+        frg_set_error(ctx, "frg_plan_create: " + err);
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    frg_plan *plan = new (std::nothrow) frg_plan();
+    if (!plan) return FRG_ERR_OUT_OF_MEMORY;
+    plan->ctx = ctx;
+    plan->nseg = n_traj;
+    plan->ntiles = static_cast<int>(hb.tile_seg.size());
+    plan->nknots = hb.nknots;
+    if (plan->nknots == 0) {
+        *out = plan;
+        return FRG_OK;
+    }
+    DeviceGuard g(ctx->device);
+    if (!plan->dev.reserve(plan->nseg + 1, plan->ntiles, err)) {
+        cudaGetLastError();
+        frg_set_error(ctx, "frg_plan_create: " + err);
+        frg_plan_destroy(plan);
+        return FRG_ERR_OUT_OF_MEMORY;
+    }
+    if (!ok(ctx, cudaMemcpy(plan->dev.segs, hb.segs.data(), sizeof(frg::Segment) * hb.segs.size(), cudaMemcpyHostToDevice),
+            "plan segment upload") ||
+        !ok(ctx, cudaMemcpy(plan->dev.tile_seg, hb.tile_seg.data(), sizeof(int) * hb.tile_seg.size(), cudaMemcpyHostToDevice),
+            "plan tile upload") ||
+        !capture(plan)) {
+        frg_plan_destroy(plan);
+        return FRG_ERR_CUDA;
+    }
+    *out = plan;
+    return FRG_OK;
+}
+
+frg_status frg_plan_create_ragged(frg_ctx *ctx, int n_traj, const int64_t *offsets, const float *q, const float *qd,
+                                  const float *u, float *dqdd, float *qdd, float *minv, frg_plan **out) {
+    if (!ctx || !out) return FRG_ERR_INVALID_ARGUMENT;
+    std::vector<frg_traj> trajs;
+    if (!frg_offsets_to_trajs(n_traj, offsets, q, qd, u, dqdd, qdd, minv, trajs)) {
+        frg_set_error(ctx, "frg_plan_create_ragged: offsets must be n_traj+1 non-decreasing values from 0");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    return frg_plan_create(ctx, n_traj, trajs.data(), out);
+}
+
+frg_status frg_plan_launch(frg_plan *plan, frg_stream stream) {
+    if (!plan) return FRG_ERR_INVALID_ARGUMENT;
+    if (plan->nknots == 0) return FRG_OK;
+    DeviceGuard g(plan->ctx->device);
+    if (!ok(plan->ctx, cudaGraphLaunch(plan->exec, stream), "cudaGraphLaunch")) return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+int64_t frg_plan_knots(const frg_plan *plan) { return plan ? plan->nknots : 0; }
+
+void frg_plan_destroy(frg_plan *plan) {
+    if (!plan) return;
+    {
+        DeviceGuard g(plan->ctx->device);
+        if (plan->exec) cudaGraphExecDestroy(plan->exec);
+        plan->dev.release();
+    }
+    delete plan;
+}
+
+frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 32 || n_knots > (int64_t(1) << 26)) {
+        frg_set_error(ctx, "frg_autotune: n_knots must be in [32, 2^26]");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    DeviceGuard g(ctx->device);
+    const size_t n = static_cast<size_t>(n_knots);
+    std::vector<float> h(21 * n);
+    std::mt19937 rng(12345);
+    std::uniform_real_distribution<float> uq(-2.0f, 2.0f), uu(-20.0f, 20.0f);
+    for (size_t i = 0; i < 14 * n; i++) h[i] = uq(rng);
+    for (size_t i = 14 * n; i < 21 * n; i++) h[i] = uu(rng);
+    float *d = nullptr;
+    if (cudaMalloc(&d, sizeof(float) * 175 * n) != cudaSuccess) {
+        cudaGetLastError();
+        frg_set_error(ctx, "frg_autotune: out of device memory");
+        return FRG_ERR_OUT_OF_MEMORY;
+    }
+    frg_traj tr{n_knots, d, d + 7 * n, d + 14 * n, d + 21 * n, d + 119 * n, d + 126 * n};
+    HostBatch hb;
+    std::string err;
+    DeviceBatch db;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaStream_t s = ctx->io_stream;
+    bool good = ok(ctx, cudaMemcpy(d, h.data(), sizeof(float) * 21 * n, cudaMemcpyHostToDevice), "autotune upload") &&
+                frg_build_batch(1, &tr, hb, err) && db.reserve(2, static_cast<int>(hb.tile_seg.size()), err) &&
+                ok(ctx, cudaMemcpy(db.segs, hb.segs.data(), sizeof(frg::Segment) * 2, cudaMemcpyHostToDevice), "upload") &&
+                ok(ctx, cudaMemcpy(db.tile_seg, hb.tile_seg.data(), sizeof(int) * hb.tile_seg.size(), cudaMemcpyHostToDevice),
+                   "upload") &&
+                ok(ctx, cudaEventCreate(&e0), "cudaEventCreate") && ok(ctx, cudaEventCreate(&e1), "cudaEventCreate");
+    const frg::LaunchShape saved = ctx->shape;
+    frg::LaunchShape best = saved;
+    float best_ms = FLT_MAX;
+    const int ntiles = static_cast<int>(hb.tile_seg.size());
+    for (int w : {1, 2, 3, 4, 6, 8}) {
+        if (!good) break;
+        const int occ = frg::max_ctas_per_sm(w);
+        if (occ < 1) continue;
+        for (int c : {occ, std::max(1, occ / 2)}) {
+            ctx->shape.warps_per_cta = w;
+            ctx->shape.ctas_per_sm = c;
+            float ms_min = FLT_MAX;
+            for (int rep = 0; rep < 5 && good; rep++) {
+                good = ok(ctx, cudaEventRecord(e0, s), "record") &&
+                       ok(ctx, frg_launch_batch(ctx, db, 1, ntiles, s), "autotune launch") &&
+                       ok(ctx, cudaEventRecord(e1, s), "record") && ok(ctx, cudaEventSynchronize(e1), "sync");
+                float ms = 0;
+                if (good && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) ms_min = std::min(ms_min, ms);
+            }
+            if (ms_min < best_ms) {
+                best_ms = ms_min;
+                best = ctx->shape;
+            }
+        }
+    }
+    if (!good && err.size()) frg_set_error(ctx, "frg_autotune: " + err);
+    ctx->shape = good ? best : saved;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    db.release();
+    cudaFree(d);
+    if (!good) return FRG_ERR_CUDA;
+    if (best_knots_per_s) *best_knots_per_s = best_ms < FLT_MAX ? static_cast<double>(n_knots) / (best_ms * 1e-3) : 0.0;
+    return FRG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,291 @@
+"""ctypes binding of the C ABI in include/frg.h (libfrg.so, built in-tree).
+
+There is no CPU fallback: if libfrg.so is missing or no CUDA device is present
+every entry point raises FrgError.
+
+The Python names mirror the reference's entry points for this path:
+``forward_dynamics_gradient`` is forwardDynamicsGradient[Threaded]
+(helpers_CPU/dynamicsGradient.h:916-934) over a batch, with q̈ and Minv
+produced on the device (forwardDynamics, :936-939, fused in), and
+``Context.gradient`` is the dynamicsGradientKernel launch of time_GPU.cu:314.
+"""
+import ctypes
+import os
+
+from .build import LIB_PATH
+
+NUM_JOINTS = 7
+DQDD_FLOATS = 98
+MINV_FLOATS = 49
+
+FRG_OK = 0
+STATUS_NAMES = {
+    0: "FRG_OK", 1: "FRG_ERR_INVALID_ARGUMENT", 2: "FRG_ERR_CUDA", 3: "FRG_ERR_OUT_OF_MEMORY",
+    4: "FRG_ERR_NOT_READY", 5: "FRG_ERR_ADMISSION", 6: "FRG_ERR_TIMEOUT", 7: "FRG_ERR_SHUTDOWN",
+    8: "FRG_ERR_NOT_FOUND", 9: "FRG_ERR_INTERNAL",
+}
+
+# every symbol include/frg.h declares (checked by tests/test_abi.py)
+EXPORTED = (
+    "frg_options_default", "frg_status_string", "frg_create", "frg_destroy", "frg_last_error",
+    "frg_set_launch_shape", "frg_get_launch_shape", "frg_gradient", "frg_gradient_host",
+    "frg_gradient_per_trajectory", "frg_gradient_batched", "frg_gradient_ragged", "frg_plan_create",
+    "frg_plan_create_ragged", "frg_plan_launch", "frg_plan_knots", "frg_plan_destroy", "frg_autotune",
+    "frg_host_alloc", "frg_host_free",
+)
+
+
+class FrgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("vel_damping", ctypes.c_int), ("mpc_mode", ctypes.c_int),
+                ("warps_per_cta", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
+
+
+class Traj(ctypes.Structure):
+    _fields_ = [("n_knots", ctypes.c_int64), ("q", ctypes.c_void_p), ("qd", ctypes.c_void_p),
+                ("u", ctypes.c_void_p), ("dqdd", ctypes.c_void_p), ("qdd", ctypes.c_void_p),
+                ("minv", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def _declare(L):
+    vp, i32, i64, st = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int
+    sig = {
+        "frg_options_default": (None, [ctypes.POINTER(Options)]),
+        "frg_status_string": (ctypes.c_char_p, [st]),
+        "frg_create": (st, [ctypes.POINTER(vp), ctypes.POINTER(Options)]),
+        "frg_destroy": (None, [vp]),
+        "frg_last_error": (ctypes.c_char_p, [vp]),
+        "frg_set_launch_shape": (st, [vp, i32, i32]),
+        "frg_get_launch_shape": (st, [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
+        "frg_gradient": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp]),
+        "frg_gradient_host": (st, [vp, i32, vp, vp, vp, vp, vp, vp]),
+        "frg_gradient_per_trajectory": (st, [vp, i32, ctypes.POINTER(Traj), vp]),
+        "frg_gradient_batched": (st, [vp, i32, ctypes.POINTER(Traj), vp]),
+        "frg_gradient_ragged": (st, [vp, i32, ctypes.POINTER(i64), vp, vp, vp, vp, vp, vp, vp]),
+        "frg_plan_create": (st, [vp, i32, ctypes.POINTER(Traj), ctypes.POINTER(vp)]),
+        "frg_plan_create_ragged": (st, [vp, i32, ctypes.POINTER(i64), vp, vp, vp, vp, vp, vp, ctypes.POINTER(vp)]),
+        "frg_plan_launch": (st, [vp, vp]),
+        "frg_plan_knots": (i64, [vp]),
+        "frg_plan_destroy": (None, [vp]),
+        "frg_autotune": (st, [vp, i64, ctypes.POINTER(ctypes.c_double)]),
+        "frg_host_alloc": (vp, [ctypes.c_size_t]),
+        "frg_host_free": (None, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def lib():
+    """The loaded libfrg.so (raises FrgError if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FrgError(9, f"{LIB_PATH} is missing: build it with __graft_entry__.build() "
+                              "(the engine is CUDA-only and has no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def _ptr(x):
+    """Device/host address of an int, a torch tensor, a numpy array or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if hasattr(x, "ctypes"):
+        return x.ctypes.data
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+def make_trajs(trajs):
+    """(ctypes array, count) from dicts/tuples (n, q, qd, u, dqdd, qdd, minv)."""
+    arr = (Traj * max(1, len(trajs)))()
+    for i, t in enumerate(trajs):
+        n, q, qd, u, dqdd, qdd, minv = t
+        arr[i] = Traj(int(n), _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd), _ptr(minv))
+    return arr, len(trajs)
+
+
+class Plan:
+    def __init__(self, ctx, handle):
+        self._ctx, self._h = ctx, handle
+
+    @property
+    def knots(self):
+        return lib().frg_plan_knots(self._h)
+
+    def launch(self, stream=None):
+        self._ctx._check(lib().frg_plan_launch(self._h, _stream_ptr(stream)), "frg_plan_launch")
+
+    def close(self):
+        if self._h:
+            lib().frg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """An engine context on one CUDA device (frg_create / frg_destroy)."""
+
+    def __init__(self, device=0, vel_damping=False, mpc_mode=False, warps_per_cta=0, ctas_per_sm=0):
+        L = lib()
+        opt = Options()
+        L.frg_options_default(ctypes.byref(opt))
+        opt.device, opt.vel_damping, opt.mpc_mode = int(device), int(bool(vel_damping)), int(bool(mpc_mode))
+        opt.warps_per_cta, opt.ctas_per_sm = int(warps_per_cta), int(ctas_per_sm)
+        h = ctypes.c_void_p()
+        st = L.frg_create(ctypes.byref(h), ctypes.byref(opt))
+        if st != FRG_OK:
+            raise FrgError(st, "frg_create: " + L.frg_last_error(None).decode())
+        self._h = h
+        self.device = device
+        self.vel_damping, self.mpc_mode = bool(vel_damping), bool(mpc_mode)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().frg_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st, what):
+        if st != FRG_OK:
+            raise FrgError(st, f"{what}: {lib().frg_last_error(self._h).decode()}")
+
+    def last_error(self):
+        return lib().frg_last_error(self._h).decode()
+
+    # ---------------------------------------------------------- shapes
+    def launch_shape(self):
+        w, c = ctypes.c_int(), ctypes.c_int()
+        self._check(lib().frg_get_launch_shape(self._h, ctypes.byref(w), ctypes.byref(c)), "frg_get_launch_shape")
+        return w.value, c.value
+
+    def set_launch_shape(self, warps_per_cta, ctas_per_sm):
+        self._check(lib().frg_set_launch_shape(self._h, int(warps_per_cta), int(ctas_per_sm)), "frg_set_launch_shape")
+
+    def autotune(self, n_knots):
+        best = ctypes.c_double()
+        self._check(lib().frg_autotune(self._h, int(n_knots), ctypes.byref(best)), "frg_autotune")
+        return best.value
+
+    # ---------------------------------------------------------- calls
+    def gradient(self, n_knots, q, qd, u, dqdd, qdd, minv, stream=None):
+        """Plain path on device buffers (addresses, torch tensors)."""
+        self._check(lib().frg_gradient(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd),
+                                       _ptr(minv), _stream_ptr(stream)), "frg_gradient")
+
+    def gradient_host_into(self, n_knots, q, qd, u, dqdd, qdd, minv):
+        """Host-buffer path: inputs in, outputs written to the given host arrays."""
+        self._check(lib().frg_gradient_host(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd),
+                                            _ptr(qdd), _ptr(minv)), "frg_gradient_host")
+
+    def gradient_host(self, q, qd, u):
+        """numpy float32 [n,7] x3 -> (dqdd [n,98], qdd [n,7], minv [n,49])."""
+        import numpy as np
+        q, qd, u = (np.ascontiguousarray(x, dtype=np.float32) for x in (q, qd, u))
+        n = q.shape[0]
+        dqdd = np.empty((n, DQDD_FLOATS), np.float32)
+        qdd = np.empty((n, NUM_JOINTS), np.float32)
+        minv = np.empty((n, MINV_FLOATS), np.float32)
+        self.gradient_host_into(n, q, qd, u, dqdd, qdd, minv)
+        return dqdd, qdd, minv
+
+    def per_trajectory(self, trajs, stream=None):
+        arr, n = make_trajs(trajs)
+        self._check(lib().frg_gradient_per_trajectory(self._h, n, arr, _stream_ptr(stream)),
+                    "frg_gradient_per_trajectory")
+
+    def batched(self, trajs, stream=None):
+        arr, n = make_trajs(trajs)
+        self._check(lib().frg_gradient_batched(self._h, n, arr, _stream_ptr(stream)), "frg_gradient_batched")
+
+    def ragged(self, offsets, q, qd, u, dqdd, qdd, minv, stream=None):
+        import numpy as np
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        self._check(lib().frg_gradient_ragged(self._h, len(off) - 1, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                              _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd), _ptr(minv),
+                                              _stream_ptr(stream)), "frg_gradient_ragged")
+
+    def plan(self, trajs):
+        arr, n = make_trajs(trajs)
+        h = ctypes.c_void_p()
+        self._check(lib().frg_plan_create(self._h, n, arr, ctypes.byref(h)), "frg_plan_create")
+        return Plan(self, h)
+
+    def plan_ragged(self, offsets, q, qd, u, dqdd, qdd, minv):
+        import numpy as np
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        h = ctypes.c_void_p()
+        self._check(lib().frg_plan_create_ragged(self._h, len(off) - 1, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                                 _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd), _ptr(minv),
+                                                 ctypes.byref(h)), "frg_plan_create_ragged")
+        return Plan(self, h)
+
+
+def forward_dynamics_gradient(q, qd, u, vel_damping=False, mpc_mode=False, ctx=None, stream=None):
+    """Batch gradient on torch CUDA tensors [n,7] (float32): returns
+    (dqdd [n,98], qdd [n,7], minv [n,49]) on the same device, asynchronously
+    on `stream` (default: torch's current stream)."""
+    import torch
+    for t in (q, qd, u):
+        if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and t.shape[-1] == NUM_JOINTS):
+            raise ValueError("q, qd, u must be contiguous float32 CUDA tensors of shape [n, 7]")
+    n = q.shape[0]
+    dev = q.device
+    own = ctx is None
+    if own:
+        ctx = Context(device=dev.index or 0, vel_damping=vel_damping, mpc_mode=mpc_mode)
+    try:
+        dqdd = torch.empty((n, DQDD_FLOATS), device=dev, dtype=torch.float32)
+        qdd = torch.empty((n, NUM_JOINTS), device=dev, dtype=torch.float32)
+        minv = torch.empty((n, MINV_FLOATS), device=dev, dtype=torch.float32)
+        st = stream if stream is not None else torch.cuda.current_stream(dev)
+        ctx.gradient(n, q, qd, u, dqdd, qdd, minv, stream=st)
+        if own:
+            st.synchronize()
+    finally:
+        if own:
+            ctx.close()
+    return dqdd, qdd, minv

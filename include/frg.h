@@ -1,0 +1,165 @@
+/*
+ * frg.h - C ABI of the GB300 (sm_103a) iiwa_14 forward-dynamics-gradient engine.
+ *
+ * Per knot point (q, qd, u) the engine runs the RNEA forward/backward sweeps,
+ * the articulated-body Minv recursion, q̈ = Minv (u - c), the dtau/dq and
+ * dtau/dqd recursions and the finish [dq̈/dq | dq̈/dq̇] = -Minv [dtau/dq | dtau/dqd],
+ * in FP32 on the CUDA cores.
+ *
+ * Replaces the host sequence of the reference's time_GPU.cu:137-158,313-316
+ * (pack [q|qd|u|qdd|Minv] per knot, cudaMemcpy H2D,
+ *  dynamicsGradientKernel<T,N,MPC_MODE,VEL_DAMPING><<<N,(32,7)>>>(d_dqdd,
+ *  d_mem_vol, d_mem_const) from helpers_GPU/dynamicsGradient.cuh:1257-1290,
+ *  cudaMemcpy D2H) with one call whose inputs are only q, qd, u: q̈ and Minv
+ * are produced on the device instead of being computed on the host by
+ * forwardDynamics (helpers_CPU/dynamicsGradient.h:686-706, :936-939).
+ *
+ * Layouts (all float32, knot-major, every matrix column-major as in the
+ * reference, helpers_CPU/dynamicsGradient.h:34-41):
+ *   q, qd, u  [n][7]
+ *   dqdd      [n][98]  = 7x14, column c < 7: dq̈/dq_c, column 7 + c: dq̈/dq̇_c
+ *                        (the reference's 2*NUM_POS*NUM_POS block per knot,
+ *                        time_CPU.cpp:34, dynamicsGradient.h:921)
+ *   qdd       [n][7]
+ *   minv      [n][49]  dense symmetric (the reference's DENSE_MINV form,
+ *                        time_GPU.cu:134)
+ *
+ * Conventions: every call returns an frg_status (nothing aborts or exits;
+ * the reference's gpuErrchk aborted the process, dynamicsGradient.cuh:28-35);
+ * frg_last_error() describes the last failure of a context.  A context is used
+ * by one host thread at a time.  Buffers passed in belong to the caller.
+ */
+#ifndef FRG_H
+#define FRG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FRG_NUM_JOINTS 7
+#define FRG_DQDD_FLOATS 98
+#define FRG_MINV_FLOATS 49
+
+typedef enum frg_status {
+    FRG_OK = 0,
+    FRG_ERR_INVALID_ARGUMENT = 1,
+    FRG_ERR_CUDA = 2,
+    FRG_ERR_OUT_OF_MEMORY = 3,
+    FRG_ERR_NOT_READY = 4,  /* a server request is still in flight */
+    FRG_ERR_ADMISSION = 5,  /* a server request can never fit the device pool */
+    FRG_ERR_TIMEOUT = 6,
+    FRG_ERR_SHUTDOWN = 7,
+    FRG_ERR_NOT_FOUND = 8,
+    FRG_ERR_INTERNAL = 9
+} frg_status;
+
+/* Same type as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st *frg_stream;
+
+typedef struct frg_ctx frg_ctx;
+typedef struct frg_plan frg_plan;
+
+/* Replaces the reference's compile-time switches (utils/experiment_helpers.h:
+ * 17-21; template bools MPC_MODE, VEL_DAMPING of dynamicsGradient.h:685,868). */
+typedef struct frg_options {
+    int device;        /* CUDA device ordinal (default 0) */
+    int vel_damping;   /* VEL_DAMPING: adds 0.5 qd to the bias and 0.5 to the
+                          dtau/dqd diagonal (default 0, experiment_helpers.h:20) */
+    int mpc_mode;      /* MPC_MODE: gravity-compensated arm, base acceleration 0
+                          (default 0, dynamicsGradient.h:635-637) */
+    int warps_per_cta; /* 0 = engine default; each warp owns 32 knots */
+    int ctas_per_sm;   /* 0 = engine default (persistent batched launches) */
+} frg_options;
+
+void frg_options_default(frg_options *opt);
+const char *frg_status_string(frg_status s);
+
+/* Creates a context on opt->device (NULL opt = defaults). */
+frg_status frg_create(frg_ctx **out, const frg_options *opt);
+void frg_destroy(frg_ctx *ctx);
+/* Message of the last failed call on ctx ("" if none).  ctx may be NULL. */
+const char *frg_last_error(const frg_ctx *ctx);
+
+/* Launch shape used by every launch of ctx (the autotuner sets it too). */
+frg_status frg_set_launch_shape(frg_ctx *ctx, int warps_per_cta, int ctas_per_sm);
+frg_status frg_get_launch_shape(const frg_ctx *ctx, int *warps_per_cta, int *ctas_per_sm);
+
+/*
+ * Plain path: one launch over n_knots knots of DEVICE arrays, asynchronous on
+ * `stream`.  The drop-in for dynamicsGradientKernel<<<N,(32,7)>>>
+ * (helpers_GPU/dynamicsGradient.cuh:1259) with q̈ and Minv produced, not
+ * consumed.  n_knots == 0 is a no-op.
+ */
+frg_status frg_gradient(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u, float *dqdd,
+                        float *qdd, float *minv, frg_stream stream);
+
+/*
+ * Same, for HOST arrays: copies the inputs in, runs, copies the outputs back
+ * through device buffers owned by ctx, and returns when the results are in
+ * the host arrays (the time_GPU.cu:313-316 "Compute + I/O" sequence).  Host
+ * arrays from frg_host_alloc() (pinned) copy fastest.
+ */
+frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                             float *dqdd, float *qdd, float *minv);
+
+/* One trajectory (a contiguous run of knots) of a batched call; all DEVICE
+ * pointers with the layouts above. */
+typedef struct frg_traj {
+    int64_t n_knots;
+    const float *q, *qd, *u;
+    float *dqdd, *qdd, *minv;
+} frg_traj;
+
+/*
+ * Plain form over many trajectories: one launch per trajectory, in order, on
+ * `stream` (what a caller of the reference does for a batch of trajectories:
+ * one dynamicsGradientKernel launch each).
+ */
+frg_status frg_gradient_per_trajectory(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_stream stream);
+
+/*
+ * Batched form: ONE persistent launch that walks the 32-knot tiles of all
+ * trajectories' knots (a ragged offset list), asynchronous on `stream`.
+ * Builds the launch's descriptor list on every call; for a batch that is run
+ * repeatedly, build an frg_plan once instead.
+ */
+frg_status frg_gradient_batched(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_stream stream);
+
+/* Convenience: trajectories as [offsets[t], offsets[t+1]) of contiguous
+ * device arrays (offsets: HOST array of n_traj + 1 non-decreasing entries). */
+frg_status frg_gradient_ragged(frg_ctx *ctx, int n_traj, const int64_t *offsets, const float *q, const float *qd,
+                               const float *u, float *dqdd, float *qdd, float *minv, frg_stream stream);
+
+/*
+ * Plans: a batched launch prepared once (descriptor list on the device, CUDA
+ * graph captured on first launch) and replayed by frg_plan_launch.  The
+ * trajectory pointers are baked in; the data behind them may change between
+ * launches.  Launches of one plan must not overlap on the device.
+ */
+frg_status frg_plan_create(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_plan **out);
+frg_status frg_plan_create_ragged(frg_ctx *ctx, int n_traj, const int64_t *offsets, const float *q,
+                                  const float *qd, const float *u, float *dqdd, float *qdd, float *minv,
+                                  frg_plan **out);
+frg_status frg_plan_launch(frg_plan *plan, frg_stream stream);
+int64_t frg_plan_knots(const frg_plan *plan);
+void frg_plan_destroy(frg_plan *plan);
+
+/*
+ * Autotuner: times every launch shape (warps per CTA x resident CTAs per SM)
+ * on n_knots synthetic knots with CUDA events and keeps the fastest in ctx.
+ * Writes the best throughput (knots/s) if best_knots_per_s is not NULL.
+ */
+frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s);
+
+/* Pinned host memory for the _host calls and the server (NULL on failure). */
+void *frg_host_alloc(size_t bytes);
+void frg_host_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FRG_H */

@@ -1,0 +1,188 @@
+/* frg oracle: CPU restatement of the reference's iiwa_14 forward-dynamics
+ * gradient (helpers_CPU/dynamicsGradient.h + helpers_CPU/minv.h), in FP64 and
+ * FP32, plus a persistent-thread-pool driver shaped like time_CPU.cpp:30-54.
+ *
+ * ORACLE TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline / reference arm load it (as oracle/libfrg_oracle.so),
+ * and only as the checker or the timed CPU baseline.  The CUDA product path
+ * never calls it and never falls back to it.
+ *
+ * Pinned against the reference itself: tests/golden/ holds outputs of the
+ * reference's own helpers_CPU code (built by oracle/Makefile into oracle/_ref/)
+ * and tests/test_oracle.py checks this file against them.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+/* g, as the reference's GRAVITY default (dynamicsGradient.h:7-9). */
+static const double kGravity = 9.81;
+
+/* Link inertial data from utils/iiwa_14.urdf (links iiwa_link_1..7, lines
+ * 31-37, 47-53, 63-69, 79-85, 95-101, 111-119, 129-137): the same constants
+ * the reference code-generates at dynamicsGradient.h:127-202.  Columns:
+ * Ixx Ixy Ixz Iyy Iyz Izz (at the COM), COM x y z, mass. */
+static const double kLinkInertial[7][10] = {
+    {0.121, 0.0, 0.0, 0.116, -0.021, 0.0175, 0.0, -0.03, 0.12, 5.76},
+    {0.0638, 0.0001, 0.00008, 0.0416, 0.0157, 0.0331, 0.0003, 0.059, 0.042, 6.35},
+    {0.0873, 0.0, 0.0, 0.083, 0.014, 0.0108, 0.0, 0.03, 0.13, 3.5},
+    {0.0368, 0.0, 0.0, 0.02045, 0.008, 0.02171, 0.0, 0.067, 0.034, 3.5},
+    {0.0318, 0.000007, 0.000027, 0.028916, 0.005586, 0.006, 0.0001, 0.021, 0.076, 3.5},
+    {0.0049, 0.0, 0.0, 0.0047, 0.0, 0.0036, 0.0, 0.0006, 0.0004, 1.8},
+    {0.0055, 0.0, 0.0, 0.0055, 0.0, 0.005, 0.0, 0.0, 0.02, 1.2},
+};
+
+/* Joint frames from utils/iiwa_14.urdf (iiwa_joint_1..7 <origin>, lines 26,
+ * 42, 58, 74, 90, 106, 124): F = R(rpy)^T as a column-major signed
+ * permutation, and the joint origin xyz in the parent frame.  rpy (0,0,0) ->
+ * identity; (pi/2,0,pi) and (-pi/2,pi,0) -> w |-> (-w0, w2, w1);
+ * (pi/2,0,0) -> w |-> (w0, w2, -w1).  Same translations as the reference's
+ * tz_j1..ty_j7 (dynamicsGradient.h:223-229). */
+static const double kJointFT[7][9] = {
+    {1, 0, 0, 0, 1, 0, 0, 0, 1},
+    {-1, 0, 0, 0, 0, 1, 0, 1, 0},
+    {-1, 0, 0, 0, 0, 1, 0, 1, 0},
+    {1, 0, 0, 0, 0, -1, 0, 1, 0},
+    {-1, 0, 0, 0, 0, 1, 0, 1, 0},
+    {1, 0, 0, 0, 0, -1, 0, 1, 0},
+    {-1, 0, 0, 0, 0, 1, 0, 1, 0},
+};
+static const double kJointOrigin[7][3] = {
+    {0, 0, 0.1575}, {0, 0, 0.2025}, {0, 0.2045, 0}, {0, 0, 0.2155},
+    {0, 0.1845, 0}, {0, 0, 0.2155}, {0, 0.081, 0},
+};
+
+#define REAL double
+#define FN(name) name##_f64
+#include "frg_oracle_impl.h"
+#undef REAL
+#undef FN
+#undef SZ6
+#undef NJ
+#define REAL float
+#define FN(name) name##_f32
+#include "frg_oracle_impl.h"
+#undef REAL
+#undef FN
+
+/* -------------------------------------------------------------- exports ---- */
+
+int frg_oracle_gradient_f64(int n, const double *q, const double *qd, const double *u, const double *fext,
+                            int damping, int mpc, double *dqdd, double *qdd, double *minv) {
+    if (n < 0) return 1;
+    for (int k = 0; k < n; k++)
+        knot_gradient_f64(&q[7 * k], &qd[7 * k], &u[7 * k], fext ? &fext[42 * k] : NULL, damping, mpc,
+                          &dqdd[98 * k], &qdd[7 * k], &minv[49 * k]);
+    return 0;
+}
+
+int frg_oracle_gradient_f32(int n, const float *q, const float *qd, const float *u, const float *fext,
+                            int damping, int mpc, float *dqdd, float *qdd, float *minv) {
+    if (n < 0) return 1;
+    for (int k = 0; k < n; k++)
+        knot_gradient_f32(&q[7 * k], &qd[7 * k], &u[7 * k], fext ? &fext[42 * k] : NULL, damping, mpc,
+                          &dqdd[98 * k], &qdd[7 * k], &minv[49 * k]);
+    return 0;
+}
+
+/* Transforms and inertias alone, for the model-constant checks. */
+void frg_oracle_model_f64(const double *q, double *X, double *I) {
+    double s[7], c[7];
+    for (int k = 0; k < 7; k++) { s[k] = sin(q[k]); c[k] = cos(q[k]); }
+    model_transforms_f64(X, s, c);
+    model_inertias_f64(I);
+}
+
+/* ---------------------------------------------- persistent worker pool ---- */
+/* Shaped like the reference's ReusableThreads (utils/ReusableThreads.h:26-115):
+ * persistent workers each take one task (a contiguous chunk of knots, as
+ * time_CPU.cpp:30-36 splits them) per round, and the caller waits for all. */
+
+typedef struct {
+    pthread_t th;
+    int tid;
+} worker_t;
+
+static struct {
+    pthread_mutex_t mu;
+    pthread_cond_t go, done;
+    int nthreads, generation, pending, shutdown;
+    int n;
+    const float *q, *qd, *u;
+    float *dqdd, *qdd, *minv;
+    worker_t *w;
+} g_pool = {.mu = PTHREAD_MUTEX_INITIALIZER, .go = PTHREAD_COND_INITIALIZER, .done = PTHREAD_COND_INITIALIZER};
+
+static void *worker_main(void *arg) {
+    worker_t *w = (worker_t *)arg;
+    int seen = 0;
+    for (;;) {
+        pthread_mutex_lock(&g_pool.mu);
+        while (!g_pool.shutdown && g_pool.generation == seen) pthread_cond_wait(&g_pool.go, &g_pool.mu);
+        if (g_pool.shutdown) { pthread_mutex_unlock(&g_pool.mu); break; }
+        seen = g_pool.generation;
+        const int n = g_pool.n, T = g_pool.nthreads;
+        pthread_mutex_unlock(&g_pool.mu);
+        const int per = n / T, k0 = per * w->tid, k1 = (w->tid == T - 1) ? n : per * (w->tid + 1);
+        if (k1 > k0)
+            frg_oracle_gradient_f32(k1 - k0, g_pool.q + 7 * k0, g_pool.qd + 7 * k0, g_pool.u + 7 * k0, NULL, 0, 0,
+                                    g_pool.dqdd + 98 * k0, g_pool.qdd + 7 * k0, g_pool.minv + 49 * k0);
+        pthread_mutex_lock(&g_pool.mu);
+        if (--g_pool.pending == 0) pthread_cond_signal(&g_pool.done);
+        pthread_mutex_unlock(&g_pool.mu);
+    }
+    return NULL;
+}
+
+static void pool_stop(void) {
+    if (!g_pool.w) return;
+    pthread_mutex_lock(&g_pool.mu);
+    g_pool.shutdown = 1;
+    pthread_cond_broadcast(&g_pool.go);
+    pthread_mutex_unlock(&g_pool.mu);
+    for (int t = 0; t < g_pool.nthreads; t++) pthread_join(g_pool.w[t].th, NULL);
+    free(g_pool.w);
+    g_pool.w = NULL;
+    g_pool.shutdown = 0;
+    g_pool.nthreads = 0;
+}
+
+static int pool_start(int threads) {
+    if (g_pool.w && g_pool.nthreads == threads) return 0;
+    pool_stop();
+    g_pool.w = (worker_t *)calloc((size_t)threads, sizeof(worker_t));
+    if (!g_pool.w) return 1;
+    g_pool.nthreads = threads;
+    for (int t = 0; t < threads; t++) {
+        g_pool.w[t].tid = t;
+        if (pthread_create(&g_pool.w[t].th, NULL, worker_main, &g_pool.w[t])) return 1;
+    }
+    return 0;
+}
+
+/* Runs `iters` rounds of the FP32 full path over n knots on `threads`
+ * persistent workers, DAMPING off / gravity on (the reference's experiment
+ * defaults, utils/experiment_helpers.h:19-20).  Returns the wall seconds of
+ * all rounds, or a negative value on error.  Not thread-safe. */
+double frg_oracle_time_threaded_f32(int n, const float *q, const float *qd, const float *u, float *dqdd,
+                                    float *qdd, float *minv, int threads, int iters) {
+    if (threads < 1 || n < 0 || iters < 0 || pool_start(threads)) return -1.0;
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int it = 0; it < iters; it++) {
+        pthread_mutex_lock(&g_pool.mu);
+        g_pool.n = n; g_pool.q = q; g_pool.qd = qd; g_pool.u = u;
+        g_pool.dqdd = dqdd; g_pool.qdd = qdd; g_pool.minv = minv;
+        g_pool.pending = threads;
+        g_pool.generation++;
+        pthread_cond_broadcast(&g_pool.go);
+        while (g_pool.pending > 0) pthread_cond_wait(&g_pool.done, &g_pool.mu);
+        pthread_mutex_unlock(&g_pool.mu);
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+void frg_oracle_pool_shutdown(void) { pool_stop(); }

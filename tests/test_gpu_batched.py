@@ -1,0 +1,115 @@
+"""Batched (persistent, ragged) and per-trajectory forms, plans / CUDA graphs
+(GPU).  Every knot's result must not depend on what it is batched with."""
+import numpy as np
+import pytest
+
+import frg
+import frg_oracle
+from conftest import TOL, max_err
+
+pytestmark = pytest.mark.gpu
+
+
+def alloc(torch, n):
+    return (torch.empty((n, 98), device="cuda"), torch.empty((n, 7), device="cuda"), torch.empty((n, 49), device="cuda"))
+
+
+def test_ragged_mix_matches_plain_bitwise():
+    import torch
+    h, off = frg.ragged_horizons(512, 8, 256, seed=2021)
+    n = int(off[-1])
+    q, qd, u = frg.sample_knots(n, seed=17)
+    tq, tqd, tu = (torch.from_numpy(x).cuda() for x in (q, qd, u))
+    with frg.Context() as ctx:
+        plain = alloc(torch, n)
+        ctx.gradient(n, tq, tqd, tu, *plain)
+        rag = alloc(torch, n)
+        ctx.ragged(off, tq, tqd, tu, *rag)
+        per = alloc(torch, n)
+        trajs = [(int(off[t + 1] - off[t]), tq[off[t]:], tqd[off[t]:], tu[off[t]:], per[0][off[t]:], per[1][off[t]:],
+                  per[2][off[t]:]) for t in range(512)]
+        ctx.per_trajectory(trajs)
+        torch.cuda.synchronize()
+    for a, b, c in zip(plain, rag, per):
+        assert torch.equal(a, b) and torch.equal(a, c)
+    idx = np.arange(0, n, 53)
+    rd, rq, rm = frg_oracle.gradient_f64(q[idx], qd[idx], u[idx])
+    assert max_err(rag[0].cpu().numpy()[idx], rd) <= TOL
+    assert max_err(rag[1].cpu().numpy()[idx], rq) <= TOL
+    assert max_err(rag[2].cpu().numpy()[idx], rm) <= TOL
+
+
+@pytest.mark.parametrize("horizons", [[1], [7], [8], [255], [256], [0, 5, 0, 33, 0], [1] * 70, [31, 1, 32, 33, 64, 2]])
+def test_edge_horizons(horizons):
+    import torch
+    off = np.concatenate([[0], np.cumsum(horizons)]).astype(np.int64)
+    n = int(off[-1])
+    q, qd, u = frg.sample_knots(max(n, 1), seed=len(horizons) + n)
+    tq, tqd, tu = (torch.from_numpy(x).cuda() for x in (q, qd, u))
+    with frg.Context() as ctx:
+        out = alloc(torch, max(n, 1))
+        ctx.ragged(off, tq, tqd, tu, *out)
+        torch.cuda.synchronize()
+    if n:
+        rd, rq, rm = frg_oracle.gradient_f64(q[:n], qd[:n], u[:n])
+        assert max_err(out[0].cpu().numpy()[:n], rd) <= TOL
+        assert max_err(out[2].cpu().numpy()[:n], rm) <= TOL
+
+
+def test_scattered_trajectories_alone_and_in_mix():
+    """Trajectories in separate buffers: each one's result alone equals its
+    result inside a 40-trajectory batch, bit for bit."""
+    import torch
+    rng = np.random.default_rng(8)
+    hs = rng.integers(1, 200, size=40)
+    bufs = []
+    for i, hh in enumerate(hs):
+        q, qd, u = frg.sample_knots(int(hh), seed=300 + i)
+        bufs.append([int(hh)] + [torch.from_numpy(x).cuda() for x in (q, qd, u)] + list(alloc(torch, int(hh))))
+    with frg.Context() as ctx:
+        ctx.batched([tuple(b) for b in bufs])
+        torch.cuda.synchronize()
+        mixed = [[t.clone() for t in b[4:]] for b in bufs]
+        for b in bufs:
+            for t in b[4:]:
+                t.zero_()
+            ctx.batched([tuple(b)])
+        torch.cuda.synchronize()
+    for b, m in zip(bufs, mixed):
+        for alone, mix in zip(b[4:], m):
+            assert torch.equal(alone, mix)
+
+
+def test_plan_graph_replay_tracks_input_changes():
+    import torch
+    h, off = frg.ragged_horizons(64, 8, 256, seed=5)
+    n = int(off[-1])
+    q, qd, u = frg.sample_knots(n, seed=6)
+    tq, tqd, tu = (torch.from_numpy(x).cuda() for x in (q, qd, u))
+    with frg.Context() as ctx:
+        out = alloc(torch, n)
+        plan = ctx.plan_ragged(off, tq, tqd, tu, *out)
+        assert plan.knots == n
+        for rep in range(3):
+            plan.launch()
+        torch.cuda.synchronize()
+        first = [t.clone() for t in out]
+        q2 = frg.perturb(q, 1e-2, seed=9)
+        tq.copy_(torch.from_numpy(q2))
+        plan.launch()
+        torch.cuda.synchronize()
+        rd, rq, rm = frg_oracle.gradient_f64(q2, qd, u)
+        assert max_err(out[0].cpu().numpy(), rd) <= TOL
+        tq.copy_(torch.from_numpy(q))
+        plan.launch()
+        torch.cuda.synchronize()
+        for a, b in zip(first, out):
+            assert torch.equal(a, b)
+        plan.close()
+
+
+def test_autotune_picks_a_valid_shape():
+    with frg.Context() as ctx:
+        kps = ctx.autotune(32768)
+        w, c = ctx.launch_shape()
+    assert kps > 0 and 1 <= w <= 8 and c >= 1

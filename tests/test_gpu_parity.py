@@ -1,0 +1,120 @@
+"""CUDA path vs the oracle and the reference's golden outputs (GPU).
+
+Bar: max Frobenius-relative error per output matrix (dqdd 7x14, qdd, Minv)
+and knot <= 1e-4 against FP64 (the reference's own FP64 outputs in
+tests/golden, and the FP64 oracle), and the same against the reference's
+FP32 outputs."""
+import numpy as np
+import pytest
+
+import frg
+import frg_oracle
+from conftest import TOL, max_err
+
+pytestmark = pytest.mark.gpu
+MODES = [(d, m) for d in (0, 1) for m in (0, 1)]
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    assert torch.cuda.is_available()
+    return torch
+
+
+@pytest.mark.parametrize("damping,mpc", MODES)
+def test_golden_all_modes(golden, damping, mpc):
+    with frg.Context(vel_damping=damping, mpc_mode=mpc) as ctx:
+        d, q, m = ctx.gradient_host(golden["q"], golden["qd"], golden["u"])
+    tag = f"f64_d{damping}_m{mpc}"
+    assert max_err(d, golden[f"dqdd_{tag}"]) <= TOL
+    assert max_err(q, golden[f"qdd_{tag}"]) <= TOL
+    assert max_err(m, golden[f"minv_{tag}"]) <= TOL
+
+
+def test_golden_against_reference_fp32(golden):
+    with frg.Context() as ctx:
+        d, q, m = ctx.gradient_host(golden["q"], golden["qd"], golden["u"])
+    assert max_err(d, golden["dqdd_f32_d0_m0"]) <= TOL
+    assert max_err(q, golden["qdd_f32_d0_m0"]) <= TOL
+    assert max_err(m, golden["minv_f32_d0_m0"]) <= TOL
+
+
+@pytest.mark.parametrize("n", [1, 7, 31, 32, 33, 95, 1000, 4097])
+def test_oracle_parity_sizes(n):
+    q, qd, u = frg.sample_knots(n, seed=1000 + n)
+    with frg.Context() as ctx:
+        d, qq, m = ctx.gradient_host(q, qd, u)
+    rd, rq, rm = frg_oracle.gradient_f64(q, qd, u)
+    assert max_err(d, rd) <= TOL and max_err(qq, rq) <= TOL and max_err(m, rm) <= TOL
+
+
+def test_device_path_equals_host_path(torch_cuda):
+    torch = torch_cuda
+    q, qd, u = frg.sample_knots(777, seed=11)
+    with frg.Context() as ctx:
+        hd, hq, hm = ctx.gradient_host(q, qd, u)
+        tq, tqd, tu = (torch.from_numpy(x).cuda() for x in (q, qd, u))
+        dd, dq, dm = frg.forward_dynamics_gradient(tq, tqd, tu, ctx=ctx)
+        torch.cuda.synchronize()
+    assert np.array_equal(dd.cpu().numpy(), hd)
+    assert np.array_equal(dq.cpu().numpy(), hq)
+    assert np.array_equal(dm.cpu().numpy(), hm)
+
+
+def test_zero_knots_is_noop():
+    with frg.Context() as ctx:
+        ctx.gradient(0, 0, 0, 0, 0, 0, 0)
+        ctx.gradient_host_into(0, None, None, None, None, None, None)
+
+
+def test_negative_knots_rejected():
+    with frg.Context() as ctx:
+        with pytest.raises(frg.FrgError) as ei:
+            ctx.gradient(-1, 0, 0, 0, 0, 0, 0)
+        assert ei.value.status == 1
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (2, 4), (3, 3), (4, 2), (8, 1)])
+def test_launch_shapes_bitwise_identical(shape):
+    q, qd, u = frg.sample_knots(1500, seed=21)
+    with frg.Context() as ctx:
+        base = ctx.gradient_host(q, qd, u)
+        ctx.set_launch_shape(*shape)
+        other = ctx.gradient_host(q, qd, u)
+    for a, b in zip(base, other):
+        assert np.array_equal(a, b)
+
+
+def test_full_size_properties(torch_cuda):
+    """N = 65536 (largest plain config): outputs finite, Minv exactly
+    symmetric and positive definite, and a strided sample within TOL of the
+    FP64 oracle."""
+    torch = torch_cuda
+    n = 65536
+    q, qd, u = frg.sample_knots(n, seed=65536)
+    with frg.Context() as ctx:
+        tq, tqd, tu = (torch.from_numpy(x).cuda() for x in (q, qd, u))
+        d, qq, m = frg.forward_dynamics_gradient(tq, tqd, tu, ctx=ctx)
+        torch.cuda.synchronize()
+    d, qq, m = d.cpu().numpy(), qq.cpu().numpy(), m.cpu().numpy()
+    assert np.isfinite(d).all() and np.isfinite(qq).all() and np.isfinite(m).all()
+    M = m.reshape(-1, 7, 7)
+    assert np.array_equal(M, M.transpose(0, 2, 1))
+    idx = np.arange(0, n, 97)
+    assert (np.linalg.eigvalsh(M[idx].astype(np.float64)) > 0).all()
+    rd, rq, rm = frg_oracle.gradient_f64(q[idx], qd[idx], u[idx])
+    assert max_err(d[idx], rd) <= TOL and max_err(qq[idx], rq) <= TOL and max_err(m[idx], rm) <= TOL
+
+
+def test_nonfinite_input_stays_in_its_knot():
+    q, qd, u = frg.sample_knots(64, seed=4)
+    q = q.copy()
+    q[5, 3] = np.nan
+    with frg.Context() as ctx:
+        d, qq, m = ctx.gradient_host(q, qd, u)
+    bad = ~np.isfinite(d).all(axis=1)
+    assert bad[5] and bad.sum() == 1
+    keep = np.arange(64) != 5
+    rd, _, _ = frg_oracle.gradient_f64(q[keep], qd[keep], u[keep])
+    assert max_err(d[keep], rd) <= TOL
