@@ -14,8 +14,10 @@ import subprocess
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REPO_ROOT = os.path.dirname(PKG_ROOT)
 CSRC = os.path.join(PKG_ROOT, "csrc")
+HOST_SRC = os.path.join(PKG_ROOT, "host")
 BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 LIB_PATH = os.path.join(PKG_ROOT, "frg", "libfrg.so")
+BIN_DIR = os.path.join(PKG_ROOT, "frg", "bin")
 INCLUDE = os.path.join(REPO_ROOT, "include")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -81,7 +83,30 @@ def build(force=False, verbose=False, ptxas_info=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of libfrg.so failed:\n{r.stdout}\n{r.stderr}")
+    build_host_tools(nvcc, force, verbose)
     return LIB_PATH
+
+
+def build_host_tools(nvcc, force=False, verbose=False):
+    """C++ drivers over the C ABI (host/*.cpp -> frg/bin/<name>), linked to libfrg.so."""
+    if not os.path.isdir(HOST_SRC):
+        return
+    os.makedirs(BIN_DIR, exist_ok=True)
+    for f in sorted(os.listdir(HOST_SRC)):
+        if not f.endswith(".cpp"):
+            continue
+        src = os.path.join(HOST_SRC, f)
+        exe = os.path.join(BIN_DIR, f[:-4])
+        if not force and not _stale(exe, [src, LIB_PATH, os.path.join(INCLUDE, "frg.h")]):
+            continue
+        cmd = [nvcc, "-O2", "-std=c++17", "-I", INCLUDE, src, "-o", exe, "-L", os.path.dirname(LIB_PATH), "-lfrg",
+               "-cudart", "shared", "-Xlinker", "-rpath,$ORIGIN/..",
+               "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"build of {f} failed:\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":
