@@ -31,7 +31,7 @@ EXPORTED = (
     "frg_set_launch_shape", "frg_get_launch_shape", "frg_gradient", "frg_gradient_host",
     "frg_gradient_per_trajectory", "frg_gradient_batched", "frg_gradient_ragged", "frg_plan_create",
     "frg_plan_create_ragged", "frg_plan_launch", "frg_plan_knots", "frg_plan_destroy", "frg_autotune",
-    "frg_host_alloc", "frg_host_free",
+    "frg_host_alloc", "frg_host_free", "frg_gradient_ragged_noalloc",
 )
 
 
@@ -78,6 +78,7 @@ def _declare(L):
         "frg_autotune": (st, [vp, i64, ctypes.POINTER(ctypes.c_double)]),
         "frg_host_alloc": (vp, [ctypes.c_size_t]),
         "frg_host_free": (None, [vp]),
+        "frg_gradient_ragged_noalloc": (st, [vp, i32, ctypes.POINTER(i64), vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

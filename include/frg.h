@@ -134,6 +134,26 @@ frg_status frg_gradient_ragged(frg_ctx *ctx, int n_traj, const int64_t *offsets,
                                const float *u, float *dqdd, float *qdd, float *minv, frg_stream stream);
 
 /*
+ * Allocation-free batched call.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc/cudaFree once running -- a real-time
+ * MPC loop (cudaFree synchronizes the device, cudaMalloc can block for an
+ * unbounded time) or a plug-in whose host application owns all device memory.
+ * Same arguments, layouts and results as frg_gradient_ragged, but the launch's
+ * descriptor lists and work counter live in one fixed 512 KiB device array
+ * that every GPU loading the library holds until process exit, so at most
+ * FRG_NOALLOC_MAX_TRAJ trajectories and FRG_NOALLOC_MAX_KNOTS knots per call
+ * (larger batches return FRG_ERR_INVALID_ARGUMENT).  The first call on a
+ * device looks up that array's device address and sets the kernel up: make it
+ * before any stream capture.  All calls share the array: calls whose launches
+ * may overlap on the GPU (different streams, unordered) race -- order them.
+ */
+#define FRG_NOALLOC_MAX_TRAJ 4096
+#define FRG_NOALLOC_MAX_KNOTS (65536 * 32)
+frg_status frg_gradient_ragged_noalloc(frg_ctx *ctx, int n_traj, const int64_t *offsets, const float *q,
+                                       const float *qd, const float *u, float *dqdd, float *qdd, float *minv,
+                                       frg_stream stream);
+
+/*
  * Plans: a batched launch prepared once (descriptor list on the device, CUDA
  * graph captured on first launch) and replayed by frg_plan_launch.  The
  * trajectory pointers are baked in; the data behind them may change between
