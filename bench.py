@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--impl", choices=["frg", "reference"], default="frg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving latency measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-traj", type=int, default=N_TRAJ, help="trajectories in the ragged mix")
+    ap.add_argument("--profile", action="store_true",
+                    help="batched launches only (no autotune, plain form, e2e, serving or CPU baseline): "
+                         "the command the ncu summaries in profiles/ capture")
     return ap.parse_args()
 
 
@@ -66,12 +70,9 @@ def dist_setup():
     return ws, rank, local
 
 
-def workload(rank):
-    import frg
-    h, off = frg.ragged_horizons(N_TRAJ, H_LO, H_HI, seed=MIX_SEED + rank)
-    n = int(off[-1])
-    q, qd, u = frg.sample_knots(n, seed=MIX_SEED * 7 + rank)
-    return h, off, n, q, qd, u
+def workload(rank, n_traj=N_TRAJ):
+    from frg import dist as fdist
+    return fdist.rank_mix(rank, n_traj, H_LO, H_HI, MIX_SEED)
 
 
 def load_peaks():
@@ -201,11 +202,12 @@ def run_frg(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
-    h, off, n, q, qd, u = workload(rank)
+    h, off, n, q, qd, u = workload(rank, args.n_traj)
+    n_traj = args.n_traj
     peaks, peaks_src = load_peaks()
 
     ctx = frg.Context(device=dev.index)
-    tuned = ctx.autotune(n)
+    tuned = None if args.profile else ctx.autotune(n)
     shape = ctx.launch_shape()
 
     stream = torch.cuda.Stream(device=dev)
@@ -218,7 +220,7 @@ def run_frg(args):
             plan = ctx.plan_ragged(off, tq, tqd, tu, *outs)
             o = [int(x) for x in off]
             trajs = [(o[t + 1] - o[t], tq[o[t]:], tqd[o[t]:], tu[o[t]:], outs[0][o[t]:], outs[1][o[t]:],
-                      outs[2][o[t]:]) for t in range(N_TRAJ)]
+                      outs[2][o[t]:]) for t in range(n_traj)]
             sets.append((tq, tqd, tu, outs, plan, trajs))
     stream.synchronize()
 
@@ -254,13 +256,18 @@ def run_frg(args):
     barrier()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
-    total_ms = sum(step_ms)
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    from frg import dist as fdist
+    value, total_ms, _ = fdist.aggregate(sum(step_ms), n, args.steps, device=dev)
     ms_per_step = total_ms / args.steps
-    value = n * ws * args.steps / (total_ms * 1e-3)
+
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile": True, "knots_per_step": n, "steps": args.steps,
+                              "launch_ms": statistics.mean(step_ms), "launch_shape": shape}))
+        for s in sets:
+            s[4].close()
+        ctx.close()
+        return 0
 
     # ---- plain per-trajectory launches ----
     for i in range(args.warmup):
@@ -283,14 +290,13 @@ def run_frg(args):
     for p in [hq, hqd, hu] + hout:
         frg.lib().frg_host_free(p)
 
-    # ---- serving latency ----
-    served = None
+    # ---- serving: latency at 50 % of saturation, and admission under a 2 GiB pool ----
+    served = served_adm = None
     if not args.no_serve:
-        try:
-            from frg import serve
-            served = serve.bench_latency(ctx, seconds=4.0)
-        except (ImportError, AttributeError):
-            served = None
+        import frg_oracle
+        from frg import serve
+        served = serve.bench_latency(ctx, seconds=3.0)
+        served_adm = serve.bench_admission(ctx, oracle=frg_oracle)
 
     line = None
     if rank == 0:
@@ -306,7 +312,7 @@ def run_frg(args):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {
-                "workload": f"ragged mix: {N_TRAJ} trajectories, horizons U{{{H_LO}..{H_HI}}} (seed {MIX_SEED}), "
+                "workload": f"ragged mix: {n_traj} trajectories, horizons U{{{H_LO}..{H_HI}}} (seed {MIX_SEED}), "
                             f"{n} knots per rank; batched persistent launch replayed as a CUDA graph",
                 "knots_per_step": n, "l2": f"{ROTATING_SETS} rotating input/output sets "
                                             f"({ROTATING_SETS * n * BYTES_PER_KNOT / 1e6:.0f} MB > 129 MB L2)",
@@ -315,10 +321,11 @@ def run_frg(args):
             },
             "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 84 * n, "d2h_bytes_per_step": 616 * n,
                     "call": "frg_gradient_host (pinned host buffers)"},
-            "plain_per_trajectory": {"value": plain_value, "unit": UNIT, "launches_per_step": N_TRAJ,
+            "plain_per_trajectory": {"value": plain_value, "unit": UNIT, "launches_per_step": n_traj,
                                      "ms_per_step": statistics.mean(plain_ms)},
             "batched_vs_plain": value / ws / plain_value,
             "served": served,
+            "served_admission": served_adm,
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                          "frac": achieved_gbs / float(peaks["hbm_gbs"]),
                          "traffic": (traffic_pk * n) if traffic_pk else None,

@@ -76,8 +76,11 @@ __global__ void __launch_bounds__(kMaxWarpsPerCta * 32)
 template <typename K>
 cudaError_t prepare(K kernel) {
     static_assert(sizeof(WarpSmem) % 16 == 0, "warp smem must keep float4 alignment");
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(sizeof(WarpSmem)) * kMaxWarpsPerCta);
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(sizeof(WarpSmem)) * kMaxWarpsPerCta);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                cudaSharedmemCarveoutMaxShared);
 }
 
 template <bool D, bool M>

@@ -14,6 +14,16 @@ struct Segment {
     long long knot_begin;
 };
 
+// One server request: a trajectory of h knots whose pinned host slot and
+// device pool slot both hold [q | qd | u | dqdd | qdd | minv] (175 h floats).
+// Inputs are read from the host slot; results go to both slots.
+struct ServeSegment {
+    float *host;
+    float *dev;
+    long long h;
+    long long knot_begin;
+};
+
 // Launch shape: warps per CTA (each warp owns 32 knots at a time) and, for the
 // persistent kernel, resident CTAs per SM.
 struct LaunchShape {
@@ -40,5 +50,11 @@ cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n
 // leaves it zero again).
 cudaError_t launch_ragged(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const Segment *segs,
                           int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream);
+
+// Server batch: like launch_ragged over ServeSegments (segs[nseg] = end
+// sentinel).
+cudaError_t launch_serve(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const ServeSegment *segs,
+                         int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream);
+cudaError_t init_serve_kernels();
 
 }  // namespace frg

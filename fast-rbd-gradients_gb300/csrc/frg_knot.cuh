@@ -44,9 +44,37 @@ __device__ __forceinline__ float *shfl_ptr(float *p, int src) {
     return reinterpret_cast<float *>(__shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), src));
 }
 
+// True when lane i's base is lane 0's base + i * STRIDE for all 32 lanes (a
+// tile of 32 consecutive knots of one array); b0 = lane 0's base.  Warp-uniform.
+template <int STRIDE, typename P>
+__device__ __forceinline__ bool tile_contiguous(P base, int lane, P &b0) {
+    b0 = shfl_ptr(base, 0);
+    const bool mine = base != nullptr && b0 != nullptr && base == b0 + lane * STRIDE;
+    return __all_sync(0xffffffffu, mine);
+}
+
+__device__ __forceinline__ bool aligned16(const void *p) {
+    return (reinterpret_cast<unsigned long long>(p) & 15ull) == 0;
+}
+
 // Coalesced gather of W floats per knot (knot-major) into stage[lane*W + j].
+// Contiguous tiles copy 32*W floats straight (float4 when aligned); other
+// tiles (idle lanes, trajectory boundaries) resolve every knot's base.
 template <int W>
 __device__ __forceinline__ void gather_in(float *stage, const float *base, int lane) {
+    const float *b0;
+    if (tile_contiguous<W>(base, lane, b0)) {
+        if (aligned16(b0)) {
+            const float4 *src = reinterpret_cast<const float4 *>(b0);
+            float4 *dst = reinterpret_cast<float4 *>(stage);
+#pragma unroll
+            for (int e = lane; e < 8 * W; e += 32) dst[e] = __ldg(src + e);
+        } else {
+#pragma unroll
+            for (int e = lane; e < 32 * W; e += 32) stage[e] = __ldg(b0 + e);
+        }
+        return;
+    }
 #pragma unroll
     for (int e = lane; e < 32 * W; e += 32) {
         const int kn = e / W, j = e - kn * W;
@@ -55,15 +83,44 @@ __device__ __forceinline__ void gather_in(float *stage, const float *base, int l
     }
 }
 
-// Coalesced scatter of stage[lane*W + j] to each knot's W floats at base.
-template <int W>
+// Coalesced scatter of stage[lane*W + j] to each knot's W floats at base
+// (knots STRIDE floats apart).
+template <int W, int STRIDE = W>
 __device__ __forceinline__ void scatter_out(const float *stage, float *base, int lane) {
     __syncwarp();
+    float *b0;
+    if (tile_contiguous<STRIDE>(base, lane, b0)) {
+        if constexpr (STRIDE == W) {
+            if (aligned16(b0)) {
+                const float4 *src = reinterpret_cast<const float4 *>(stage);
+                float4 *dst = reinterpret_cast<float4 *>(b0);
+#pragma unroll
+                for (int e = lane; e < 8 * W; e += 32) dst[e] = src[e];
+            } else {
 #pragma unroll 7
-    for (int e = lane; e < 32 * W; e += 32) {
-        const int kn = e / W, j = e - kn * W;
-        float *p = shfl_ptr(base, kn);
-        if (p) p[j] = stage[e];
+                for (int e = lane; e < 32 * W; e += 32) b0[e] = stage[e];
+            }
+        } else {
+            // element e = lane + 32 m is knot e / W, entry e % W
+            int kn = lane / W, j = lane - (lane / W) * W;
+#pragma unroll 7
+            for (int e = lane; e < 32 * W; e += 32) {
+                b0[kn * STRIDE + j] = stage[e];
+                kn += 32 / W;
+                j += 32 % W;
+                if (j >= W) {
+                    j -= W;
+                    kn++;
+                }
+            }
+        }
+    } else {
+#pragma unroll 7
+        for (int e = lane; e < 32 * W; e += 32) {
+            const int kn = e / W, j = e - kn * W;
+            float *p = shfl_ptr(base, kn);
+            if (p) p[j] = stage[e];
+        }
     }
     __syncwarp();
 }
@@ -79,6 +136,14 @@ __device__ __forceinline__ void sts_link(WarpSmem *ws, int k, int lane, const fl
     ws->link[kSlotsPerLink * k + 0][lane] = make_float4(v[0], v[1], v[2], v[3]);
     ws->link[kSlotsPerLink * k + 1][lane] = make_float4(v[4], v[5], Iv[0], Iv[1]);
     ws->link[kSlotsPerLink * k + 2][lane] = make_float4(Iv[2], Iv[3], Iv[4], Iv[5]);
+}
+
+// sin and cos of a joint angle: the hardware approximation inside [-pi, pi]
+// (absolute error below 2^-21, far inside the 1e-4 parity bar), the
+// range-reducing library routine outside it.
+__device__ __forceinline__ void sincos_angle(float x, float *s, float *c) {
+    if (fabsf(x) <= 3.14159f) __sincosf(x, s, c);
+    else sincosf(x, s, c);
 }
 
 // ------------------------------------------------ articulated inertia ------
@@ -197,7 +262,7 @@ template <bool DAMP, bool MPC>
 __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7], const float qd[7], const float u[7],
                                        float sq[7], float cq[7], float Mi[7][7], float qdd[7]) {
 #pragma unroll
-    for (int k = 0; k < kJoints; k++) sincosf(q[k], &sq[k], &cq[k]);
+    for (int k = 0; k < kJoints; k++) sincos_angle(q[k], &sq[k], &cq[k]);
 
     // RNEA forward with qdd = 0 (RNEA_fp, dynamicsGradient.h:620-659)
     float f[kJoints][6];
@@ -468,9 +533,13 @@ __device__ __forceinline__ void minv_times(float out[7], const float Mi[7][7], c
     }
 }
 
-// Full path for the 32 knots of one warp tile.
-template <bool DAMP, bool MPC>
-__device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotPtrs &kp) {
+// Full path for the 32 knots of one warp tile.  With MIRROR, every input and
+// output is also stored at the `mr` pointers (the server keeps a resident
+// device copy of each trajectory while reading inputs from / writing results
+// to its pinned host slot).
+template <bool DAMP, bool MPC, bool MIRROR = false>
+__device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotPtrs &kp,
+                                             const KnotPtrs &mr = KnotPtrs{}) {
     float q[7], qd[7], u[7];
     gather_in<7>(ws->stage, kp.q, lane);
     gather_in<7>(ws->stage + 224, kp.qd, lane);
@@ -483,6 +552,11 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
         u[j] = ws->stage[448 + lane * 7 + j];
     }
     __syncwarp();
+    if constexpr (MIRROR) {
+        scatter_out<7>(ws->stage, const_cast<float *>(mr.q), lane);
+        scatter_out<7>(ws->stage + 224, const_cast<float *>(mr.qd), lane);
+        scatter_out<7>(ws->stage + 448, const_cast<float *>(mr.u), lane);
+    }
 
     float sq[7], cq[7], Mi[7][7], qdd[7];
     phase1<DAMP, MPC>(ws, lane, q, qd, u, sq, cq, Mi, qdd);
@@ -493,9 +567,11 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r + 7 * c] = r <= c ? Mi[r][c] : Mi[c][r];
     scatter_out<49>(ws->stage, kp.minv, lane);
+    if constexpr (MIRROR) scatter_out<49>(ws->stage, mr.minv, lane);
 #pragma unroll
     for (int r = 0; r < 7; r++) ws->stage[lane * 7 + r] = qdd[r];
     scatter_out<7>(ws->stage, kp.qdd, lane);
+    if constexpr (MIRROR) scatter_out<7>(ws->stage, mr.qdd, lane);
 
     rnea_with_qdd<MPC>(ws, lane, qd, qdd, sq, cq);
     __syncwarp();
@@ -512,7 +588,8 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
     }
-    scatter_out<49>(ws->stage, kp.dqdd, lane);
+    scatter_out<49, 98>(ws->stage, kp.dqdd, lane);
+    if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd, lane);
     // d qdd / dqd: columns 7..13
 #pragma unroll 1
     for (int c = 0; c < kJoints; c++) {
@@ -522,7 +599,8 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
     }
-    scatter_out<49>(ws->stage, kp.dqdd ? kp.dqdd + 49 : nullptr, lane);
+    scatter_out<49, 98>(ws->stage, kp.dqdd ? kp.dqdd + 49 : nullptr, lane);
+    if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd ? mr.dqdd + 49 : nullptr, lane);
 }
 
 }  // namespace frg

@@ -1,0 +1,87 @@
+// Server kernel: the batched persistent kernel over server slots.  Inputs
+// come from each request's pinned host slot (read over the host link,
+// coalesced), results are written to the host slot and to the trajectory's
+// resident device pool slot, so a batch needs no per-request copy.
+#include "frg_kernels.cuh"
+#include "frg_knot.cuh"
+
+namespace frg {
+
+namespace {
+
+__device__ __forceinline__ KnotPtrs slot_knot(float *base, long long h, long long i) {
+    return KnotPtrs{base + 7 * i, base + 7 * h + 7 * i, base + 14 * h + 7 * i, base + 21 * h + 98 * i,
+                    base + 119 * h + 7 * i, base + 126 * h + 49 * i};
+}
+
+template <bool DAMP, bool MPC>
+__global__ void __launch_bounds__(8 * 32)
+    grad_serve_kernel(const ServeSegment *segs, int nseg, const int *tile_seg, int ntiles, unsigned int *counter) {
+    extern __shared__ float4 smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    const unsigned int total_warps = gridDim.x * (blockDim.x >> 5);
+    for (;;) {
+        unsigned int ticket = 0;
+        if (lane == 0) ticket = atomicAdd(counter, 1u);
+        ticket = __shfl_sync(0xffffffffu, ticket, 0);
+        if (ticket >= static_cast<unsigned int>(ntiles)) {
+            if (lane == 0 && ticket == static_cast<unsigned int>(ntiles) + total_warps - 1u) atomicExch(counter, 0u);
+            return;
+        }
+        const long long g = static_cast<long long>(ticket) * 32 + lane;
+        KnotPtrs kp{}, mr{};
+        if (g < segs[nseg].knot_begin) {
+            int s = tile_seg[ticket];
+            while (s + 1 < nseg && segs[s + 1].knot_begin <= g) s++;
+            const ServeSegment &sg = segs[s];
+            const long long i = g - sg.knot_begin;
+            kp = slot_knot(sg.host, sg.h, i);
+            mr = slot_knot(sg.dev, sg.h, i);
+        }
+        process_tile<DAMP, MPC, true>(ws, lane, kp, mr);
+    }
+}
+
+template <bool D, bool M>
+cudaError_t set_smem() {
+    cudaError_t e = cudaFuncSetAttribute(grad_serve_kernel<D, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(sizeof(WarpSmem)) * 8);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(grad_serve_kernel<D, M>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                cudaSharedmemCarveoutMaxShared);
+}
+
+template <bool D, bool M>
+cudaError_t serve_impl(const LaunchShape &sh, int num_sms, const ServeSegment *segs, int nseg, const int *tile_seg,
+                       int ntiles, unsigned int *counter, cudaStream_t st) {
+    const int warps = sh.warps_per_cta;
+    int grid = num_sms * sh.ctas_per_sm;
+    const int needed = (ntiles + warps - 1) / warps;
+    if (grid > needed) grid = needed;
+    if (grid < 1) grid = 1;
+    grad_serve_kernel<D, M><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(segs, nseg, tile_seg, ntiles, counter);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t init_serve_kernels() {
+    cudaError_t e = cudaSuccess;
+    for (cudaError_t r : {set_smem<false, false>(), set_smem<true, false>(), set_smem<false, true>(),
+                          set_smem<true, true>()})
+        if (r != cudaSuccess && e == cudaSuccess) e = r;
+    return e;
+}
+
+cudaError_t launch_serve(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const ServeSegment *segs,
+                         int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream) {
+    if (ntiles <= 0) return cudaSuccess;
+    if (shape.warps_per_cta < 1 || shape.warps_per_cta > 8 || shape.ctas_per_sm < 1) return cudaErrorInvalidValue;
+    if (!damping && !mpc) return serve_impl<false, false>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
+    if (damping && !mpc) return serve_impl<true, false>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
+    if (!damping && mpc) return serve_impl<false, true>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
+    return serve_impl<true, true>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
+}
+
+}  // namespace frg

@@ -12,6 +12,7 @@ from .native import (  # noqa: F401
     Context,
     FrgError,
     Plan,
+    Server,
     forward_dynamics_gradient,
     lib,
 )

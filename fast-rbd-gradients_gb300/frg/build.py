@@ -88,7 +88,9 @@ def build(force=False, verbose=False, ptxas_info=False):
 
 
 def build_host_tools(nvcc, force=False, verbose=False):
-    """C++ drivers over the C ABI (host/*.cpp -> frg/bin/<name>), linked to libfrg.so."""
+    """C++ host code over the C ABI, linked to libfrg.so: host/lib<name>.cpp ->
+    frg/lib<name>.so (libraries bench.py drives), other host/*.cpp ->
+    frg/bin/<name> (executables)."""
     if not os.path.isdir(HOST_SRC):
         return
     os.makedirs(BIN_DIR, exist_ok=True)
@@ -96,12 +98,15 @@ def build_host_tools(nvcc, force=False, verbose=False):
         if not f.endswith(".cpp"):
             continue
         src = os.path.join(HOST_SRC, f)
-        exe = os.path.join(BIN_DIR, f[:-4])
-        if not force and not _stale(exe, [src, LIB_PATH, os.path.join(INCLUDE, "frg.h")]):
+        shared = f.startswith("lib")
+        out = os.path.join(os.path.dirname(LIB_PATH), f[:-4] + ".so") if shared else os.path.join(BIN_DIR, f[:-4])
+        if not force and not _stale(out, [src, LIB_PATH, os.path.join(INCLUDE, "frg.h")]):
             continue
-        cmd = [nvcc, "-O2", "-std=c++17", "-I", INCLUDE, src, "-o", exe, "-L", os.path.dirname(LIB_PATH), "-lfrg",
-               "-cudart", "shared", "-Xlinker", "-rpath,$ORIGIN/..",
-               "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+        rpath = "-rpath,$ORIGIN" if shared else "-rpath,$ORIGIN/.."
+        cmd = [nvcc, "-O2", "-std=c++17", "-I", INCLUDE, src, "-o", out, "-L", os.path.dirname(LIB_PATH), "-lfrg",
+               "-cudart", "shared", "-Xlinker", rpath, "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+        if shared:
+            cmd[1:1] = ["-shared", "-Xcompiler", "-fPIC"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

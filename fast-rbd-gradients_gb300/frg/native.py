@@ -31,7 +31,9 @@ EXPORTED = (
     "frg_set_launch_shape", "frg_get_launch_shape", "frg_gradient", "frg_gradient_host",
     "frg_gradient_per_trajectory", "frg_gradient_batched", "frg_gradient_ragged", "frg_plan_create",
     "frg_plan_create_ragged", "frg_plan_launch", "frg_plan_knots", "frg_plan_destroy", "frg_autotune",
-    "frg_host_alloc", "frg_host_free", "frg_gradient_ragged_noalloc",
+    "frg_host_alloc", "frg_host_free", "frg_gradient_ragged_noalloc", "frg_server_options_default",
+    "frg_server_create", "frg_server_destroy", "frg_server_submit", "frg_server_poll", "frg_server_wait",
+    "frg_server_wait_any", "frg_server_release", "frg_server_get_stats",
 )
 
 
@@ -50,6 +52,30 @@ class Traj(ctypes.Structure):
     _fields_ = [("n_knots", ctypes.c_int64), ("q", ctypes.c_void_p), ("qd", ctypes.c_void_p),
                 ("u", ctypes.c_void_p), ("dqdd", ctypes.c_void_p), ("qdd", ctypes.c_void_p),
                 ("minv", ctypes.c_void_p)]
+
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("pool_bytes", ctypes.c_size_t), ("max_batch_knots", ctypes.c_int), ("max_inflight", ctypes.c_int),
+                ("warps_per_cta", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
+
+
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("request_id", ctypes.c_uint64), ("traj_id", ctypes.c_uint64), ("horizon", ctypes.c_int64),
+                ("status", ctypes.c_int), ("dqdd", _fp), ("qdd", _fp), ("minv", _fp), ("dev_q", ctypes.c_void_p),
+                ("dev_qd", ctypes.c_void_p), ("dev_u", ctypes.c_void_p), ("dev_dqdd", ctypes.c_void_p),
+                ("dev_qdd", ctypes.c_void_p), ("dev_minv", ctypes.c_void_p), ("latency_us", ctypes.c_double),
+                ("queue_us", ctypes.c_double), ("batch_id", ctypes.c_uint64), ("batch_requests", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("launches", ctypes.c_uint64),
+                ("knots", ctypes.c_uint64), ("admission_stalls", ctypes.c_uint64), ("rejected", ctypes.c_uint64),
+                ("pool_bytes_cap", ctypes.c_size_t), ("pool_bytes_used", ctypes.c_size_t),
+                ("pool_bytes_peak", ctypes.c_size_t), ("queued_admission", ctypes.c_size_t),
+                ("queued_ready", ctypes.c_size_t)]
 
 
 _lib = None
@@ -79,6 +105,15 @@ def _declare(L):
         "frg_host_alloc": (vp, [ctypes.c_size_t]),
         "frg_host_free": (None, [vp]),
         "frg_gradient_ragged_noalloc": (st, [vp, i32, ctypes.POINTER(i64), vp, vp, vp, vp, vp, vp, vp]),
+        "frg_server_options_default": (None, [ctypes.POINTER(ServerOptions)]),
+        "frg_server_create": (st, [vp, ctypes.POINTER(ServerOptions), ctypes.POINTER(vp)]),
+        "frg_server_destroy": (None, [vp]),
+        "frg_server_submit": (st, [vp, ctypes.c_uint64, i64, vp, vp, vp, ctypes.POINTER(ctypes.c_uint64)]),
+        "frg_server_poll": (st, [vp, ctypes.c_uint64, ctypes.POINTER(RequestInfo)]),
+        "frg_server_wait": (st, [vp, ctypes.c_uint64, i64, ctypes.POINTER(RequestInfo)]),
+        "frg_server_wait_any": (st, [vp, i64, ctypes.POINTER(RequestInfo)]),
+        "frg_server_release": (st, [vp, ctypes.c_uint64]),
+        "frg_server_get_stats": (st, [vp, ctypes.POINTER(ServerStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -263,6 +298,70 @@ class Context:
                                                  _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd), _ptr(minv),
                                                  ctypes.byref(h)), "frg_plan_create_ragged")
         return Plan(self, h)
+
+
+class Server:
+    """Continuous-batching server on a context (frg_server_*)."""
+
+    def __init__(self, ctx, pool_bytes=1 << 30, max_batch_knots=1 << 16, max_inflight=3, warps_per_cta=0,
+                 ctas_per_sm=0):
+        L = lib()
+        opt = ServerOptions()
+        L.frg_server_options_default(ctypes.byref(opt))
+        opt.pool_bytes, opt.max_batch_knots, opt.max_inflight = int(pool_bytes), int(max_batch_knots), int(max_inflight)
+        opt.warps_per_cta, opt.ctas_per_sm = int(warps_per_cta), int(ctas_per_sm)
+        h = ctypes.c_void_p()
+        ctx._check(L.frg_server_create(ctx.handle, ctypes.byref(opt), ctypes.byref(h)), "frg_server_create")
+        self._ctx, self._h = ctx, h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().frg_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, traj_id, q, qd, u):
+        """Queue one call; returns (status, request_id).  q, qd, u: float32 [h, 7]."""
+        rid = ctypes.c_uint64()
+        st = lib().frg_server_submit(self._h, int(traj_id), int(q.shape[0]), q.ctypes.data, qd.ctypes.data,
+                                     u.ctypes.data, ctypes.byref(rid))
+        return st, rid.value
+
+    def wait(self, request_id, timeout_us=-1):
+        info = RequestInfo()
+        st = lib().frg_server_wait(self._h, int(request_id), int(timeout_us), ctypes.byref(info))
+        return st, info
+
+    def poll(self, request_id):
+        info = RequestInfo()
+        st = lib().frg_server_poll(self._h, int(request_id), ctypes.byref(info))
+        return st, info
+
+    def wait_any(self, timeout_us=-1):
+        info = RequestInfo()
+        st = lib().frg_server_wait_any(self._h, int(timeout_us), ctypes.byref(info))
+        return st, info
+
+    def release(self, traj_id):
+        return lib().frg_server_release(self._h, int(traj_id))
+
+    def stats(self):
+        s = ServerStats()
+        lib().frg_server_get_stats(self._h, ctypes.byref(s))
+        return {f: getattr(s, f) for f, _ in ServerStats._fields_}
+
+    @staticmethod
+    def results(info):
+        """Copies of (dqdd [h,98], qdd [h,7], minv [h,49]) from a completed call's info."""
+        import numpy as np
+        h = info.horizon
+        return tuple(np.ctypeslib.as_array(p, shape=(h, w)).copy()
+                     for p, w in ((info.dqdd, DQDD_FLOATS), (info.qdd, NUM_JOINTS), (info.minv, MINV_FLOATS)))
 
 
 def forward_dynamics_gradient(q, qd, u, vel_damping=False, mpc_mode=False, ctx=None, stream=None):

@@ -174,6 +174,76 @@ void frg_plan_destroy(frg_plan *plan);
  */
 frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s);
 
+/*
+ * Continuous-batching server (MPC / iLQR callers).  No counterpart in the
+ * reference, whose drivers time one synchronous batch at a time
+ * (time_GPU.cu:310-330); it serves the gradient calls of many trajectories as
+ * they arrive:
+ *  - a trajectory (traj_id) keeps a slot of 700 B per knot -- its q, qd, u
+ *    and its results -- in a capped device pool, mirrored in pinned host
+ *    memory, from its first call until frg_server_release;
+ *  - admission is by free pool bytes: a new trajectory that does not fit
+ *    waits (an admission stall) until releases make room;
+ *  - a dispatcher thread folds all ready calls into the next persistent
+ *    launch (up to max_batch_knots) while up to max_inflight earlier launches
+ *    still run, each on its own stream;
+ *  - results of a call are bit-identical alone or batched with any others.
+ * One call per trajectory may be in flight; submit copies the inputs.
+ */
+typedef struct frg_server frg_server;
+
+typedef struct frg_server_options {
+    size_t pool_bytes;    /* device pool cap (and pinned host mirror), default 1 GiB */
+    int max_batch_knots;  /* knots folded into one launch at most, default 65536 */
+    int max_inflight;     /* launches in flight at once (streams), default 3, <= 16 */
+    int warps_per_cta;    /* launch shape of server launches, 0 = the context's */
+    int ctas_per_sm;
+} frg_server_options;
+
+typedef struct frg_request_info {
+    uint64_t request_id, traj_id;
+    int64_t horizon;
+    frg_status status;
+    /* results in pinned host memory, valid until this trajectory's next
+     * submit or its release; NULL unless status == FRG_OK */
+    const float *dqdd, *qdd, *minv;
+    /* the trajectory's resident device copy (inputs and results) */
+    const float *dev_q, *dev_qd, *dev_u, *dev_dqdd, *dev_qdd, *dev_minv;
+    double latency_us;  /* submit -> results visible in host memory */
+    double queue_us;    /* submit -> launch */
+    uint64_t batch_id;
+    int batch_requests; /* calls folded into the same launch */
+} frg_request_info;
+
+typedef struct frg_server_stats {
+    uint64_t submitted, completed, launches, knots;
+    uint64_t admission_stalls; /* calls that waited for pool space */
+    uint64_t rejected;         /* calls that can never fit */
+    size_t pool_bytes_cap, pool_bytes_used, pool_bytes_peak;
+    size_t queued_admission, queued_ready;
+} frg_server_stats;
+
+void frg_server_options_default(frg_server_options *opt);
+frg_status frg_server_create(frg_ctx *ctx, const frg_server_options *opt, frg_server **out);
+/* Finishes queued and in-flight calls (calls still waiting for admission end
+ * with FRG_ERR_SHUTDOWN), then frees everything. */
+void frg_server_destroy(frg_server *srv);
+/* Queues one gradient call of trajectory traj_id over `horizon` knots (host
+ * arrays [horizon][7], copied before return).  FRG_ERR_NOT_READY if the
+ * trajectory already has a call in flight, FRG_ERR_ADMISSION if its slot can
+ * never fit the pool. */
+frg_status frg_server_submit(frg_server *srv, uint64_t traj_id, int64_t horizon, const float *q, const float *qd,
+                             const float *u, uint64_t *request_id);
+/* FRG_OK (done, info filled, request retired), FRG_ERR_NOT_READY, FRG_ERR_NOT_FOUND. */
+frg_status frg_server_poll(frg_server *srv, uint64_t request_id, frg_request_info *info);
+/* Blocks until the call is done (timeout_us < 0: no limit); FRG_ERR_TIMEOUT otherwise. */
+frg_status frg_server_wait(frg_server *srv, uint64_t request_id, int64_t timeout_us, frg_request_info *info);
+/* Next completed call not yet taken by poll/wait, in completion order. */
+frg_status frg_server_wait_any(frg_server *srv, int64_t timeout_us, frg_request_info *info);
+/* Frees the trajectory's slots (FRG_ERR_NOT_READY while a call is in flight). */
+frg_status frg_server_release(frg_server *srv, uint64_t traj_id);
+frg_status frg_server_get_stats(frg_server *srv, frg_server_stats *out);
+
 /* Pinned host memory for the _host calls and the server (NULL on failure). */
 void *frg_host_alloc(size_t bytes);
 void frg_host_free(void *p);
