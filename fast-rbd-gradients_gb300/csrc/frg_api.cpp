@@ -131,6 +131,7 @@ void frg_options_default(frg_options *opt) {
     opt->mpc_mode = 0;
     opt->warps_per_cta = 0;
     opt->ctas_per_sm = 0;
+    opt->lanes_per_knot = 0;
 }
 
 const char *frg_status_string(frg_status s) {
@@ -168,7 +169,8 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
         frg_set_error(nullptr, "frg_create: device ordinal out of range");
         return FRG_ERR_INVALID_ARGUMENT;
     }
-    if (opt.warps_per_cta < 0 || opt.warps_per_cta > frg::max_warps_per_cta() || opt.ctas_per_sm < 0) {
+    if (opt.warps_per_cta < 0 || opt.warps_per_cta > frg::max_warps_per_cta() || opt.ctas_per_sm < 0 ||
+        (opt.lanes_per_knot != 0 && opt.lanes_per_knot != 1 && opt.lanes_per_knot != 8)) {
         frg_set_error(nullptr, "frg_create: invalid launch shape");
         return FRG_ERR_INVALID_ARGUMENT;
     }
@@ -181,6 +183,8 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
     cudaDeviceProp prop;
     if (!check(ctx, cudaGetDeviceProperties(&prop, ctx->device), "cudaGetDeviceProperties") ||
         !check(ctx, frg::init_kernels(), "kernel set-up") ||
+        !check(ctx, frg::init_group_kernels(), "latency kernel set-up") ||
+        !check(ctx, frg::init_ext_kernels(), "fext / forward-dynamics kernel set-up") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !check(ctx, cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming), "cudaEventCreate")) {
         g_orphan_error = ctx->err;
@@ -191,6 +195,7 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
     ctx->shape = frg::default_shape();
     if (opt.warps_per_cta) ctx->shape.warps_per_cta = opt.warps_per_cta;
     if (opt.ctas_per_sm) ctx->shape.ctas_per_sm = opt.ctas_per_sm;
+    if (opt.lanes_per_knot) ctx->shape.lanes_per_knot = opt.lanes_per_knot;
     *out = ctx;
     return FRG_OK;
 }
@@ -222,6 +227,18 @@ frg_status frg_set_launch_shape(frg_ctx *ctx, int warps_per_cta, int ctas_per_sm
     return FRG_OK;
 }
 
+frg_status frg_set_lanes_per_knot(frg_ctx *ctx, int lanes_per_knot) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (lanes_per_knot != 1 && lanes_per_knot != 8) {
+        frg_set_error(ctx, "frg_set_lanes_per_knot: 1 (throughput mapping) or 8 (latency mapping)");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    ctx->shape.lanes_per_knot = lanes_per_knot;
+    return FRG_OK;
+}
+
+int frg_get_lanes_per_knot(const frg_ctx *ctx) { return ctx ? ctx->shape.lanes_per_knot : 0; }
+
 frg_status frg_get_launch_shape(const frg_ctx *ctx, int *warps_per_cta, int *ctas_per_sm) {
     if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
     if (warps_per_cta) *warps_per_cta = ctx->shape.warps_per_cta;
@@ -240,6 +257,53 @@ frg_status frg_gradient(frg_ctx *ctx, int n_knots, const float *q, const float *
     DeviceGuard g(ctx->device);
     if (!check(ctx, frg::launch_plain(ctx->damping, ctx->mpc, ctx->shape, n_knots, q, qd, u, dqdd, qdd, minv, stream),
                "frg_gradient launch"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+frg_status frg_gradient_fext(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                             const float *fext, float *dqdd, float *qdd, float *minv, frg_stream stream) {
+    if (!fext) return frg_gradient(ctx, n_knots, q, qd, u, dqdd, qdd, minv, stream);
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 0 || (n_knots > 0 && !(q && qd && u && dqdd && qdd && minv))) {
+        frg_set_error(ctx, "frg_gradient_fext: negative n_knots or null pointer");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n_knots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    if (!check(ctx, frg::launch_ext(ctx->damping, ctx->mpc, ctx->shape, n_knots, q, qd, u, fext, dqdd, qdd, minv, false,
+                                    stream),
+               "frg_gradient_fext launch"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+frg_status frg_forward_dynamics(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                                const float *fext, float *qdd, float *minv, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 0 || (n_knots > 0 && !(q && qd && u && qdd))) {
+        frg_set_error(ctx, "frg_forward_dynamics: negative n_knots or null pointer");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n_knots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    if (!check(ctx, frg::launch_ext(ctx->damping, ctx->mpc, ctx->shape, n_knots, q, qd, u, fext, nullptr, qdd, minv, true,
+                                    stream),
+               "frg_forward_dynamics launch"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+frg_status frg_discrete_jacobians(frg_ctx *ctx, int n_knots, const float *dqdd, const float *minv, float dt, float *A,
+                                  float *B, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 0 || (n_knots > 0 && !(dqdd && minv && A && B)) || !(dt == dt)) {
+        frg_set_error(ctx, "frg_discrete_jacobians: negative n_knots, null pointer or NaN dt");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n_knots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    if (!check(ctx, frg::launch_discretize(n_knots, dqdd, minv, dt, A, B, stream), "frg_discrete_jacobians launch"))
         return FRG_ERR_CUDA;
     return FRG_OK;
 }

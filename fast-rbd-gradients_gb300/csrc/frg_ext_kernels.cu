@@ -1,0 +1,118 @@
+// Plain-path variants either side of the gradient:
+//   - the gradient with external link forces (fext, the s_fext of the
+//     reference's RNEA_fp, helpers_CPU/dynamicsGradient.h:654-657);
+//   - forward dynamics only: q̈ and Minv (forwardDynamics, :686-706);
+//   - discrete-time Jacobians of one explicit-Euler step from the gradient:
+//       x = [q; qd],  x+ = x + dt [qd; q̈(q, qd, u)]
+//       A = dx+/dx = I + dt [0 I; dq̈/dq dq̈/dqd]   (14 x 14, column-major)
+//       B = dx+/du = dt [0; Minv]                 (14 x 7, column-major)
+#include "frg_kernels.cuh"
+#include "frg_knot.cuh"
+
+namespace frg {
+
+namespace {
+
+template <bool DAMP, bool MPC, bool FEXT, bool FDONLY>
+__global__ void __launch_bounds__(8 * 32)
+    grad_ext_kernel(const float *q, const float *qd, const float *u, const float *fext, float *dqdd, float *qdd,
+                    float *minv, int n) {
+    extern __shared__ float4 smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    const int wpc = blockDim.x >> 5, ntiles = (n + 31) / 32;
+    for (int tile = blockIdx.x * wpc + warp; tile < ntiles; tile += gridDim.x * wpc) {
+        const long long g = static_cast<long long>(tile) * 32 + lane;
+        KnotPtrs kp{};
+        if (g < n) {
+            kp = KnotPtrs{q + 7 * g, qd + 7 * g, u + 7 * g, dqdd ? dqdd + 98 * g : nullptr, qdd + 7 * g,
+                          minv ? minv + 49 * g : nullptr, FEXT ? fext + 42 * g : nullptr};
+        }
+        process_tile<DAMP, MPC, false, FEXT, FDONLY>(ws, lane, kp);
+    }
+}
+
+// One thread per output float: A [n][196] then B [n][98].
+__global__ void discretize_kernel(int n, const float *dqdd, const float *minv, float dt, float *A, float *B) {
+    const long long total = static_cast<long long>(n) * 294;
+    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<long long>(gridDim.x) * blockDim.x) {
+        if (e < static_cast<long long>(n) * 196) {
+            const long long k = e / 196;
+            const int idx = static_cast<int>(e - k * 196), r = idx % 14, c = idx / 14;
+            float v;
+            if (r < 7) v = (c == r + 7) ? dt : 0.0f;  // dq+/dqd = dt I
+            else v = dt * dqdd[98 * k + (r - 7) + 7 * c];
+            A[e] = v + (r == c ? 1.0f : 0.0f);
+        } else {
+            const long long e2 = e - static_cast<long long>(n) * 196, k = e2 / 98;
+            const int idx = static_cast<int>(e2 - k * 98), r = idx % 14, c = idx / 14;
+            B[e2] = r < 7 ? 0.0f : dt * minv[49 * k + (r - 7) + 7 * c];
+        }
+    }
+}
+
+template <typename K>
+cudaError_t opt_in(K kernel) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(sizeof(WarpSmem)) * 8);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+}
+
+template <bool D, bool M, bool F, bool O>
+cudaError_t launch_one(const LaunchShape &sh, int n, const float *q, const float *qd, const float *u,
+                       const float *fext, float *dqdd, float *qdd, float *minv, cudaStream_t st) {
+    const int w = sh.warps_per_cta, ntiles = (n + 31) / 32, grid = (ntiles + w - 1) / w;
+    grad_ext_kernel<D, M, F, O><<<grid, w * 32, sizeof(WarpSmem) * w, st>>>(q, qd, u, fext, dqdd, qdd, minv, n);
+    return cudaGetLastError();
+}
+
+template <bool F, bool O>
+cudaError_t dispatch(bool d, bool m, const LaunchShape &sh, int n, const float *q, const float *qd, const float *u,
+                     const float *fext, float *dqdd, float *qdd, float *minv, cudaStream_t st) {
+    if (!d && !m) return launch_one<false, false, F, O>(sh, n, q, qd, u, fext, dqdd, qdd, minv, st);
+    if (d && !m) return launch_one<true, false, F, O>(sh, n, q, qd, u, fext, dqdd, qdd, minv, st);
+    if (!d && m) return launch_one<false, true, F, O>(sh, n, q, qd, u, fext, dqdd, qdd, minv, st);
+    return launch_one<true, true, F, O>(sh, n, q, qd, u, fext, dqdd, qdd, minv, st);
+}
+
+}  // namespace
+
+cudaError_t init_ext_kernels() {
+    cudaError_t e = cudaSuccess;
+#define FRG_OPT(F, O)                                                                                        \
+    for (cudaError_t r : {opt_in(grad_ext_kernel<false, false, F, O>), opt_in(grad_ext_kernel<true, false, F, O>), \
+                          opt_in(grad_ext_kernel<false, true, F, O>), opt_in(grad_ext_kernel<true, true, F, O>)})  \
+        if (r != cudaSuccess && e == cudaSuccess) e = r;
+    FRG_OPT(true, false)
+    FRG_OPT(false, true)
+    FRG_OPT(true, true)
+#undef FRG_OPT
+    return e;
+}
+
+cudaError_t launch_ext(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
+                       const float *u, const float *fext, float *dqdd, float *qdd, float *minv, bool fd_only,
+                       cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    if (shape.warps_per_cta < 1 || shape.warps_per_cta > 8) return cudaErrorInvalidValue;
+    LaunchShape sh = shape;
+    if (fd_only) {
+        return fext ? dispatch<true, true>(damping, mpc, sh, n, q, qd, u, fext, nullptr, qdd, minv, stream)
+                    : dispatch<false, true>(damping, mpc, sh, n, q, qd, u, nullptr, nullptr, qdd, minv, stream);
+    }
+    return dispatch<true, false>(damping, mpc, sh, n, q, qd, u, fext, dqdd, qdd, minv, stream);
+}
+
+cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float dt, float *A, float *B,
+                              cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const long long total = static_cast<long long>(n) * 294;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    discretize_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(n, dqdd, minv, dt, A, B);
+    return cudaGetLastError();
+}
+
+}  // namespace frg

@@ -120,7 +120,8 @@ cudaError_t init_kernels() {
 }
 int max_warps_per_cta() { return kMaxWarpsPerCta; }
 
-int max_ctas_per_sm(int warps) {
+int max_ctas_per_sm(int warps, int lanes_per_knot) {
+    if (lanes_per_knot == 8) return max_group_ctas_per_sm(warps);
     int blocks = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, grad_ragged_kernel<false, false>, warps * 32,
                                                       sizeof(WarpSmem) * warps) != cudaSuccess) {
@@ -134,6 +135,7 @@ cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n
                          const float *u, float *dqdd, float *qdd, float *minv, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
     if (shape.warps_per_cta < 1 || shape.warps_per_cta > kMaxWarpsPerCta) return cudaErrorInvalidValue;
+    if (shape.lanes_per_knot == 8) return launch_group_plain(damping, mpc, shape, n, q, qd, u, dqdd, qdd, minv, stream);
     const PlainArgs a{q, qd, u, dqdd, qdd, minv, n};
     if (!damping && !mpc) return plain_impl<false, false>(shape, a, stream);
     if (damping && !mpc) return plain_impl<true, false>(shape, a, stream);
@@ -146,6 +148,8 @@ cudaError_t launch_ragged(bool damping, bool mpc, const LaunchShape &shape, int 
     if (ntiles <= 0) return cudaSuccess;
     if (shape.warps_per_cta < 1 || shape.warps_per_cta > kMaxWarpsPerCta || shape.ctas_per_sm < 1)
         return cudaErrorInvalidValue;
+    if (shape.lanes_per_knot == 8)
+        return launch_group_ragged(damping, mpc, shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
     if (!damping && !mpc) return ragged_impl<false, false>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
     if (damping && !mpc) return ragged_impl<true, false>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
     if (!damping && mpc) return ragged_impl<false, true>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);

@@ -29,6 +29,7 @@ struct ServeSegment {
 struct LaunchShape {
     int warps_per_cta = 2;
     int ctas_per_sm = 4;
+    int lanes_per_knot = 1;  // 1: knot per lane (throughput), 8: knot per 8 lanes (latency)
 };
 
 size_t warp_smem_bytes();
@@ -37,7 +38,7 @@ size_t warp_smem_bytes();
 cudaError_t init_kernels();
 int max_warps_per_cta();
 // Resident CTAs per SM of the batched kernel at `warps` warps per CTA.
-int max_ctas_per_sm(int warps);
+int max_ctas_per_sm(int warps, int lanes_per_knot = 1);
 
 // Plain path: n knots, contiguous arrays, grid over 32-knot tiles.
 cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
@@ -56,5 +57,27 @@ cudaError_t launch_ragged(bool damping, bool mpc, const LaunchShape &shape, int 
 cudaError_t launch_serve(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const ServeSegment *segs,
                          int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream);
 cudaError_t init_serve_kernels();
+
+// Latency mapping (8 lanes per knot), same arguments as the launches above.
+cudaError_t init_group_kernels();
+size_t group_warp_smem_bytes();
+int max_group_ctas_per_sm(int warps);
+cudaError_t launch_group_plain(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q,
+                               const float *qd, const float *u, float *dqdd, float *qdd, float *minv,
+                               cudaStream_t stream);
+cudaError_t launch_group_ragged(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const Segment *segs,
+                                int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream);
+cudaError_t launch_group_serve(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const ServeSegment *segs,
+                               int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream);
+
+// Plain-path variants (frg_ext_kernels.cu): gradient with external forces
+// (fext [n][7][6], link frames), forward dynamics only (fd_only: q̈, optional
+// Minv), and the explicit-Euler discrete Jacobians A [n][196], B [n][98].
+cudaError_t init_ext_kernels();
+cudaError_t launch_ext(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
+                       const float *u, const float *fext, float *dqdd, float *qdd, float *minv, bool fd_only,
+                       cudaStream_t stream);
+cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float dt, float *A, float *B,
+                              cudaStream_t stream);
 
 }  // namespace frg

@@ -34,6 +34,7 @@ struct WarpSmem {
 struct KnotPtrs {
     const float *q, *qd, *u;
     float *dqdd, *qdd, *minv;
+    const float *fext = nullptr;  // [7][6] external spatial force per link (link frame), optional
 };
 
 __device__ __forceinline__ const float *shfl_ptr(const float *p, int src) {
@@ -258,9 +259,10 @@ __device__ __forceinline__ void add_link_inertia(float A[3][3], float B[3][3], f
 
 // sincos, RNEA(q, qd, 0), bias, Minv (upper triangle, Mi[i][j] for i <= j), qdd.
 // Leaves v_k and I_k v_k of every link in the warp's link slots.
-template <bool DAMP, bool MPC>
+template <bool DAMP, bool MPC, bool FEXT = false>
 __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7], const float qd[7], const float u[7],
-                                       float sq[7], float cq[7], float Mi[7][7], float qdd[7]) {
+                                       float sq[7], float cq[7], float Mi[7][7], float qdd[7],
+                                       const float *fx = nullptr) {
 #pragma unroll
     for (int k = 0; k < kJoints; k++) sincos_angle(q[k], &sq[k], &cq[k]);
 
@@ -295,6 +297,10 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
             imul<k>(Iv, v);
             imul<k>(f[k], a);
             crf_acc(f[k], v, Iv);
+            if constexpr (FEXT) {  // f_k -= fext_k (RNEA_fp, dynamicsGradient.h:654-657)
+#pragma unroll
+                for (int i = 0; i < 6; i++) f[k][i] -= fx[6 * k + i];
+            }
             sts_link(ws, k, lane, v, Iv);
         });
     }
@@ -404,9 +410,9 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
 // RNEA(q, qd, qdd) forward + backward: stores (X_k a_{k-1})[0,1,3,4] and the
 // accumulated f_k[0,1,3,4] in the link slots (read at the diagonal step of the
 // d/dq sweeps).
-template <bool MPC>
+template <bool MPC, bool FEXT = false>
 __device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const float qd[7], const float qdd[7],
-                                              const float sq[7], const float cq[7]) {
+                                              const float sq[7], const float cq[7], const float *fx = nullptr) {
     float f[kJoints][6];
     float a[6];
     static_for<0, kJoints>([&](auto K) {
@@ -435,6 +441,10 @@ __device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const floa
         }
         imul<k>(f[k], a);
         crf_acc(f[k], v, Iv);
+        if constexpr (FEXT) {
+#pragma unroll
+            for (int i = 0; i < 6; i++) f[k][i] -= fx[6 * k + i];
+        }
     });
     static_for_down<kJoints - 1, 1>([&](auto K) {
         constexpr int k = decltype(K)::value;
@@ -536,8 +546,9 @@ __device__ __forceinline__ void minv_times(float out[7], const float Mi[7][7], c
 // Full path for the 32 knots of one warp tile.  With MIRROR, every input and
 // output is also stored at the `mr` pointers (the server keeps a resident
 // device copy of each trajectory while reading inputs from / writing results
-// to its pinned host slot).
-template <bool DAMP, bool MPC, bool MIRROR = false>
+// to its pinned host slot).  With FEXT, kp.fext holds each knot's external
+// link forces; with FDONLY only q̈ and Minv are produced (forward dynamics).
+template <bool DAMP, bool MPC, bool MIRROR = false, bool FEXT = false, bool FDONLY = false>
 __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotPtrs &kp,
                                              const KnotPtrs &mr = KnotPtrs{}) {
     float q[7], qd[7], u[7];
@@ -557,9 +568,17 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
         scatter_out<7>(ws->stage + 224, const_cast<float *>(mr.qd), lane);
         scatter_out<7>(ws->stage + 448, const_cast<float *>(mr.u), lane);
     }
+    const float *fx = nullptr;
+    if constexpr (FEXT) {  // the lane's 42 external-force floats stay staged through both RNEA passes
+        gather_in<42>(ws->stage, kp.fext, lane);
+        __syncwarp();
+        fx = ws->stage + lane * 42;
+    }
 
     float sq[7], cq[7], Mi[7][7], qdd[7];
-    phase1<DAMP, MPC>(ws, lane, q, qd, u, sq, cq, Mi, qdd);
+    phase1<DAMP, MPC, FEXT>(ws, lane, q, qd, u, sq, cq, Mi, qdd, fx);
+    if constexpr (!FDONLY) rnea_with_qdd<MPC, FEXT>(ws, lane, qd, qdd, sq, cq, fx);
+    __syncwarp();
 
     // Minv (dense) and qdd out
 #pragma unroll
@@ -572,9 +591,7 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     for (int r = 0; r < 7; r++) ws->stage[lane * 7 + r] = qdd[r];
     scatter_out<7>(ws->stage, kp.qdd, lane);
     if constexpr (MIRROR) scatter_out<7>(ws->stage, mr.qdd, lane);
-
-    rnea_with_qdd<MPC>(ws, lane, qd, qdd, sq, cq);
-    __syncwarp();
+    if constexpr (FDONLY) return;
 
     // d qdd / dq: columns 0..6 (column 0 is identically zero for this model:
     // the base joint axis is parallel to gravity, as dynamicsGradient.h:797-813 uses)

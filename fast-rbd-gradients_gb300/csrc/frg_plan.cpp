@@ -151,13 +151,15 @@ frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s)
     frg::LaunchShape best = saved;
     float best_ms = FLT_MAX;
     const int ntiles = static_cast<int>(hb.tile_seg.size());
+    for (int lanes : {1, 8})
     for (int w : {1, 2, 3, 4, 6, 8}) {
         if (!good) break;
-        const int occ = frg::max_ctas_per_sm(w);
+        const int occ = frg::max_ctas_per_sm(w, lanes);
         if (occ < 1) continue;
         for (int c : {occ, std::max(1, occ / 2)}) {
             ctx->shape.warps_per_cta = w;
             ctx->shape.ctas_per_sm = c;
+            ctx->shape.lanes_per_knot = lanes;
             float ms_min = FLT_MAX;
             for (int rep = 0; rep < 5 && good; rep++) {
                 good = ok(ctx, cudaEventRecord(e0, s), "record") &&

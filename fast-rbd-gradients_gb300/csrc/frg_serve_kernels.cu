@@ -78,6 +78,8 @@ cudaError_t launch_serve(bool damping, bool mpc, const LaunchShape &shape, int n
                          int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream) {
     if (ntiles <= 0) return cudaSuccess;
     if (shape.warps_per_cta < 1 || shape.warps_per_cta > 8 || shape.ctas_per_sm < 1) return cudaErrorInvalidValue;
+    if (shape.lanes_per_knot == 8)
+        return launch_group_serve(damping, mpc, shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
     if (!damping && !mpc) return serve_impl<false, false>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
     if (damping && !mpc) return serve_impl<true, false>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);
     if (!damping && mpc) return serve_impl<false, true>(shape, num_sms, segs, nseg, tile_seg, ntiles, counter, stream);

@@ -135,7 +135,8 @@ struct Batch {
 struct frg_server {
     frg_ctx *ctx = nullptr;
     frg_server_options opt{};
-    frg::LaunchShape shape;
+    frg::LaunchShape shape;          // batches above latency_mapping_max_knots
+    frg::LaunchShape latency_shape;  // 8 lanes per knot, for small batches
     float *dev_pool = nullptr;
     float *host_pool = nullptr;
     ArenaAllocator arena;
@@ -330,8 +331,10 @@ void frg_server::launch_batch(Batch &b, std::unique_lock<std::mutex> &lk) {
     lk.unlock();
     cudaError_t e = cudaMemcpyAsync(b.d_desc, b.h_desc, tiles_off + sizeof(int) * ntiles, cudaMemcpyHostToDevice,
                                     b.stream);
+    frg::LaunchShape sh = shape;
+    if (begin <= opt.latency_mapping_max_knots) sh = latency_shape;
     if (e == cudaSuccess)
-        e = frg::launch_serve(ctx->damping, ctx->mpc, shape, ctx->num_sms,
+        e = frg::launch_serve(ctx->damping, ctx->mpc, sh, ctx->num_sms,
                               reinterpret_cast<const frg::ServeSegment *>(b.d_desc), nseg,
                               reinterpret_cast<const int *>(b.d_desc + tiles_off), ntiles, b.d_counter, b.stream);
     if (e == cudaSuccess) e = cudaEventRecord(b.done, b.stream);
@@ -351,6 +354,7 @@ void frg_server_options_default(frg_server_options *opt) {
     opt->max_inflight = 3;
     opt->warps_per_cta = 0;
     opt->ctas_per_sm = 0;
+    opt->latency_mapping_max_knots = 4096;
 }
 
 frg_status frg_server_create(frg_ctx *ctx, const frg_server_options *opt_in, frg_server **out) {
@@ -371,6 +375,10 @@ frg_status frg_server_create(frg_ctx *ctx, const frg_server_options *opt_in, frg
     s->shape = ctx->shape;
     if (opt.warps_per_cta) s->shape.warps_per_cta = opt.warps_per_cta;
     if (opt.ctas_per_sm) s->shape.ctas_per_sm = opt.ctas_per_sm;
+    if (s->shape.lanes_per_knot == 8) s->shape.lanes_per_knot = 1;  // big batches: throughput mapping
+    s->latency_shape.warps_per_cta = 4;
+    s->latency_shape.ctas_per_sm = std::max(1, frg::max_ctas_per_sm(4, 8));
+    s->latency_shape.lanes_per_knot = 8;
     s->max_tiles_per_batch = opt.max_batch_knots / 32 + 2;
     s->max_reqs_per_batch = std::min(opt.max_batch_knots, 8192);
     DeviceGuard g(ctx->device);
@@ -382,6 +390,7 @@ frg_status frg_server_create(frg_ctx *ctx, const frg_server_options *opt_in, frg
     };
     cudaError_t e;
     if ((e = frg::init_serve_kernels()) != cudaSuccess) return fail("kernel set-up", e);
+    if ((e = frg::init_group_kernels()) != cudaSuccess) return fail("latency kernel set-up", e);
     if ((e = cudaMalloc(&s->dev_pool, opt.pool_bytes)) != cudaSuccess) return fail("device pool", e);
     if ((e = cudaHostAlloc(&s->host_pool, opt.pool_bytes, cudaHostAllocMapped | cudaHostAllocPortable)) != cudaSuccess)
         return fail("host arena", e);

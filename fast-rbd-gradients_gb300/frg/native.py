@@ -28,12 +28,13 @@ STATUS_NAMES = {
 # every symbol include/frg.h declares (checked by tests/test_abi.py)
 EXPORTED = (
     "frg_options_default", "frg_status_string", "frg_create", "frg_destroy", "frg_last_error",
-    "frg_set_launch_shape", "frg_get_launch_shape", "frg_gradient", "frg_gradient_host",
+    "frg_set_launch_shape", "frg_get_launch_shape", "frg_set_lanes_per_knot", "frg_get_lanes_per_knot", "frg_gradient", "frg_gradient_host",
     "frg_gradient_per_trajectory", "frg_gradient_batched", "frg_gradient_ragged", "frg_plan_create",
     "frg_plan_create_ragged", "frg_plan_launch", "frg_plan_knots", "frg_plan_destroy", "frg_autotune",
     "frg_host_alloc", "frg_host_free", "frg_gradient_ragged_noalloc", "frg_server_options_default",
     "frg_server_create", "frg_server_destroy", "frg_server_submit", "frg_server_poll", "frg_server_wait",
-    "frg_server_wait_any", "frg_server_release", "frg_server_get_stats",
+    "frg_server_wait_any", "frg_server_release", "frg_server_get_stats", "frg_gradient_fext",
+    "frg_forward_dynamics", "frg_discrete_jacobians",
 )
 
 
@@ -45,7 +46,7 @@ class FrgError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("vel_damping", ctypes.c_int), ("mpc_mode", ctypes.c_int),
-                ("warps_per_cta", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
+                ("warps_per_cta", ctypes.c_int), ("ctas_per_sm", ctypes.c_int), ("lanes_per_knot", ctypes.c_int)]
 
 
 class Traj(ctypes.Structure):
@@ -56,7 +57,8 @@ class Traj(ctypes.Structure):
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("pool_bytes", ctypes.c_size_t), ("max_batch_knots", ctypes.c_int), ("max_inflight", ctypes.c_int),
-                ("warps_per_cta", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
+                ("warps_per_cta", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
+                ("latency_mapping_max_knots", ctypes.c_int)]
 
 
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -91,6 +93,8 @@ def _declare(L):
         "frg_last_error": (ctypes.c_char_p, [vp]),
         "frg_set_launch_shape": (st, [vp, i32, i32]),
         "frg_get_launch_shape": (st, [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
+        "frg_set_lanes_per_knot": (st, [vp, i32]),
+        "frg_get_lanes_per_knot": (i32, [vp]),
         "frg_gradient": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp]),
         "frg_gradient_host": (st, [vp, i32, vp, vp, vp, vp, vp, vp]),
         "frg_gradient_per_trajectory": (st, [vp, i32, ctypes.POINTER(Traj), vp]),
@@ -114,6 +118,9 @@ def _declare(L):
         "frg_server_wait_any": (st, [vp, i64, ctypes.POINTER(RequestInfo)]),
         "frg_server_release": (st, [vp, ctypes.c_uint64]),
         "frg_server_get_stats": (st, [vp, ctypes.POINTER(ServerStats)]),
+        "frg_gradient_fext": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "frg_forward_dynamics": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp]),
+        "frg_discrete_jacobians": (st, [vp, i32, vp, vp, ctypes.c_float, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -190,12 +197,13 @@ class Plan:
 class Context:
     """An engine context on one CUDA device (frg_create / frg_destroy)."""
 
-    def __init__(self, device=0, vel_damping=False, mpc_mode=False, warps_per_cta=0, ctas_per_sm=0):
+    def __init__(self, device=0, vel_damping=False, mpc_mode=False, warps_per_cta=0, ctas_per_sm=0, lanes_per_knot=0):
         L = lib()
         opt = Options()
         L.frg_options_default(ctypes.byref(opt))
         opt.device, opt.vel_damping, opt.mpc_mode = int(device), int(bool(vel_damping)), int(bool(mpc_mode))
         opt.warps_per_cta, opt.ctas_per_sm = int(warps_per_cta), int(ctas_per_sm)
+        opt.lanes_per_knot = int(lanes_per_knot)
         h = ctypes.c_void_p()
         st = L.frg_create(ctypes.byref(h), ctypes.byref(opt))
         if st != FRG_OK:
@@ -241,6 +249,12 @@ class Context:
     def set_launch_shape(self, warps_per_cta, ctas_per_sm):
         self._check(lib().frg_set_launch_shape(self._h, int(warps_per_cta), int(ctas_per_sm)), "frg_set_launch_shape")
 
+    def lanes_per_knot(self):
+        return lib().frg_get_lanes_per_knot(self._h)
+
+    def set_lanes_per_knot(self, lanes):
+        self._check(lib().frg_set_lanes_per_knot(self._h, int(lanes)), "frg_set_lanes_per_knot")
+
     def autotune(self, n_knots):
         best = ctypes.c_double()
         self._check(lib().frg_autotune(self._h, int(n_knots), ctypes.byref(best)), "frg_autotune")
@@ -251,6 +265,21 @@ class Context:
         """Plain path on device buffers (addresses, torch tensors)."""
         self._check(lib().frg_gradient(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd),
                                        _ptr(minv), _stream_ptr(stream)), "frg_gradient")
+
+    def gradient_fext(self, n_knots, q, qd, u, fext, dqdd, qdd, minv, stream=None):
+        """Gradient with external link forces fext [n][7][6] (device buffers)."""
+        self._check(lib().frg_gradient_fext(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(fext), _ptr(dqdd),
+                                            _ptr(qdd), _ptr(minv), _stream_ptr(stream)), "frg_gradient_fext")
+
+    def forward_dynamics(self, n_knots, q, qd, u, qdd, minv=None, fext=None, stream=None):
+        """q̈ (and Minv if given) only (device buffers)."""
+        self._check(lib().frg_forward_dynamics(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(fext), _ptr(qdd),
+                                               _ptr(minv), _stream_ptr(stream)), "frg_forward_dynamics")
+
+    def discrete_jacobians(self, n_knots, dqdd, minv, dt, A, B, stream=None):
+        """Explicit-Euler A [n][14x14], B [n][14x7] from dqdd and minv (device buffers)."""
+        self._check(lib().frg_discrete_jacobians(self._h, int(n_knots), _ptr(dqdd), _ptr(minv), float(dt), _ptr(A),
+                                                 _ptr(B), _stream_ptr(stream)), "frg_discrete_jacobians")
 
     def gradient_host_into(self, n_knots, q, qd, u, dqdd, qdd, minv):
         """Host-buffer path: inputs in, outputs written to the given host arrays."""
@@ -304,12 +333,14 @@ class Server:
     """Continuous-batching server on a context (frg_server_*)."""
 
     def __init__(self, ctx, pool_bytes=1 << 30, max_batch_knots=1 << 16, max_inflight=3, warps_per_cta=0,
-                 ctas_per_sm=0):
+                 ctas_per_sm=0, latency_mapping_max_knots=None):
         L = lib()
         opt = ServerOptions()
         L.frg_server_options_default(ctypes.byref(opt))
         opt.pool_bytes, opt.max_batch_knots, opt.max_inflight = int(pool_bytes), int(max_batch_knots), int(max_inflight)
         opt.warps_per_cta, opt.ctas_per_sm = int(warps_per_cta), int(ctas_per_sm)
+        if latency_mapping_max_knots is not None:
+            opt.latency_mapping_max_knots = int(latency_mapping_max_knots)
         h = ctypes.c_void_p()
         ctx._check(L.frg_server_create(ctx.handle, ctypes.byref(opt), ctypes.byref(h)), "frg_server_create")
         self._ctx, self._h = ctx, h

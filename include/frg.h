@@ -70,8 +70,11 @@ typedef struct frg_options {
                           dtau/dqd diagonal (default 0, experiment_helpers.h:20) */
     int mpc_mode;      /* MPC_MODE: gravity-compensated arm, base acceleration 0
                           (default 0, dynamicsGradient.h:635-637) */
-    int warps_per_cta; /* 0 = engine default; each warp owns 32 knots */
+    int warps_per_cta; /* 0 = engine default */
     int ctas_per_sm;   /* 0 = engine default (persistent batched launches) */
+    int lanes_per_knot; /* 0 = default (1); 1 = one knot per lane, 32 knots per
+                           warp (throughput); 8 = one knot per 8 lanes, 4 knots
+                           per warp (latency: small batches finish ~2.5x sooner) */
 } frg_options;
 
 void frg_options_default(frg_options *opt);
@@ -86,6 +89,9 @@ const char *frg_last_error(const frg_ctx *ctx);
 /* Launch shape used by every launch of ctx (the autotuner sets it too). */
 frg_status frg_set_launch_shape(frg_ctx *ctx, int warps_per_cta, int ctas_per_sm);
 frg_status frg_get_launch_shape(const frg_ctx *ctx, int *warps_per_cta, int *ctas_per_sm);
+/* Threads per knot of every launch of ctx: 1 or 8 (the autotuner sets it too). */
+frg_status frg_set_lanes_per_knot(frg_ctx *ctx, int lanes_per_knot);
+int frg_get_lanes_per_knot(const frg_ctx *ctx);
 
 /*
  * Plain path: one launch over n_knots knots of DEVICE arrays, asynchronous on
@@ -104,6 +110,26 @@ frg_status frg_gradient(frg_ctx *ctx, int n_knots, const float *q, const float *
  */
 frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
                              float *dqdd, float *qdd, float *minv);
+
+/*
+ * Either side of the gradient (plain path, DEVICE arrays, asynchronous):
+ *  - frg_gradient_fext: the gradient with external spatial forces on the links,
+ *    fext [n][7][6] (link k's force in its own frame, [n, f] order), subtracted
+ *    from each link force in both RNEA passes as the reference's s_fext
+ *    (helpers_CPU/dynamicsGradient.h:654-657); fext == NULL is frg_gradient.
+ *  - frg_forward_dynamics: q̈ [n][7] and, if minv != NULL, Minv [n][49] only
+ *    (forwardDynamics, dynamicsGradient.h:686-706); fext may be NULL.
+ *  - frg_discrete_jacobians: for the explicit-Euler step x+ = x + dt [qd; q̈]
+ *    of the state x = [q; qd], A = I + dt [0 I; dq̈/dq dq̈/dqd] [n][14x14] and
+ *    B = dt [0; Minv] [n][14x7], column-major, from dqdd and minv (the solver
+ *    step that consumes the gradient; MPC/iLQR callers).
+ */
+frg_status frg_gradient_fext(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                             const float *fext, float *dqdd, float *qdd, float *minv, frg_stream stream);
+frg_status frg_forward_dynamics(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                                const float *fext, float *qdd, float *minv, frg_stream stream);
+frg_status frg_discrete_jacobians(frg_ctx *ctx, int n_knots, const float *dqdd, const float *minv, float dt,
+                                  float *A, float *B, frg_stream stream);
 
 /* One trajectory (a contiguous run of knots) of a batched call; all DEVICE
  * pointers with the layouts above. */
@@ -168,8 +194,9 @@ int64_t frg_plan_knots(const frg_plan *plan);
 void frg_plan_destroy(frg_plan *plan);
 
 /*
- * Autotuner: times every launch shape (warps per CTA x resident CTAs per SM)
- * on n_knots synthetic knots with CUDA events and keeps the fastest in ctx.
+ * Autotuner: times every launch shape (threads per knot x warps per CTA x
+ * resident CTAs per SM) on n_knots synthetic knots with CUDA events and keeps
+ * the fastest in ctx.
  * Writes the best throughput (knots/s) if best_knots_per_s is not NULL.
  */
 frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s);
@@ -196,8 +223,10 @@ typedef struct frg_server_options {
     size_t pool_bytes;    /* device pool cap (and pinned host mirror), default 1 GiB */
     int max_batch_knots;  /* knots folded into one launch at most, default 65536 */
     int max_inflight;     /* launches in flight at once (streams), default 3, <= 16 */
-    int warps_per_cta;    /* launch shape of server launches, 0 = the context's */
+    int warps_per_cta;    /* launch shape of larger server launches, 0 = the context's */
     int ctas_per_sm;
+    int latency_mapping_max_knots; /* batches up to this many knots use the
+                                      8-lanes-per-knot mapping (default 4096) */
 } frg_server_options;
 
 typedef struct frg_request_info {

@@ -113,3 +113,25 @@ def test_autotune_picks_a_valid_shape():
         kps = ctx.autotune(32768)
         w, c = ctx.launch_shape()
     assert kps > 0 and 1 <= w <= 8 and c >= 1
+
+
+def test_latency_mapping_ragged_and_plan():
+    import torch
+    h, off = frg.ragged_horizons(100, 1, 64, seed=12)
+    n = int(off[-1])
+    q, qd, u = frg.sample_knots(n, seed=13)
+    tq, tqd, tu = (torch.from_numpy(x).cuda() for x in (q, qd, u))
+    with frg.Context(lanes_per_knot=8) as ctx:
+        out = alloc(torch, n)
+        ctx.ragged(off, tq, tqd, tu, *out)
+        out2 = alloc(torch, n)
+        plan = ctx.plan_ragged(off, tq, tqd, tu, *out2)
+        plan.launch()
+        plan.launch()
+        torch.cuda.synchronize()
+        plan.close()
+    rd, rq, rm = frg_oracle.gradient_f64(q, qd, u)
+    for o in (out, out2):
+        assert max_err(o[0].cpu().numpy(), rd) <= TOL
+        assert max_err(o[1].cpu().numpy(), rq) <= TOL
+        assert max_err(o[2].cpu().numpy(), rm) <= TOL

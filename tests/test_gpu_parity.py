@@ -118,3 +118,23 @@ def test_nonfinite_input_stays_in_its_knot():
     keep = np.arange(64) != 5
     rd, _, _ = frg_oracle.gradient_f64(q[keep], qd[keep], u[keep])
     assert max_err(d[keep], rd) <= TOL
+
+
+@pytest.mark.parametrize("damping,mpc", MODES)
+@pytest.mark.parametrize("n", [1, 5, 37, 1000])
+def test_latency_mapping_parity(golden, damping, mpc, n):
+    """8 lanes per knot (latency mapping): same results as the throughput
+    mapping and within TOL of the FP64 oracle."""
+    q, qd, u = frg.sample_knots(n, seed=70 + n)
+    with frg.Context(vel_damping=damping, mpc_mode=mpc) as ctx:
+        a = ctx.gradient_host(q, qd, u)
+        ctx.set_lanes_per_knot(8)
+        assert ctx.lanes_per_knot() == 8
+        b = ctx.gradient_host(q, qd, u)
+        g = ctx.gradient_host(golden["q"], golden["qd"], golden["u"])
+    rd, rq, rm = frg_oracle.gradient_f64(q, qd, u, damping, mpc)
+    assert max_err(b[0], rd) <= TOL and max_err(b[1], rq) <= TOL and max_err(b[2], rm) <= TOL
+    for x, y in zip(a, b):
+        assert max_err(x, y) <= 1e-5
+    tag = f"f64_d{damping}_m{mpc}"
+    assert max_err(g[0], golden[f"dqdd_{tag}"]) <= TOL and max_err(g[2], golden[f"minv_{tag}"]) <= TOL
