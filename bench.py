@@ -210,6 +210,16 @@ def run_frg(args):
     tuned = None if args.profile else ctx.autotune(n)
     shape = ctx.launch_shape()
 
+    # Trajectories live in memory in a shuffled order (as separately produced
+    # trajectories do), so the batch is a ragged list of scattered runs that
+    # the persistent kernel walks; the plain form launches once per trajectory
+    # over the same buffers.
+    perm = np.random.Generator(np.random.PCG64(MIX_SEED)).permutation(n_traj)
+    mem_off = np.zeros(n_traj, np.int64)
+    pos = 0
+    for t in perm:
+        mem_off[t] = pos
+        pos += int(off[t + 1] - off[t])
     stream = torch.cuda.Stream(device=dev)
     sets = []
     with torch.cuda.stream(stream):
@@ -217,10 +227,10 @@ def run_frg(args):
             qq = frg.perturb(q, 1e-3, seed=i) if i else q
             tq, tqd, tu = (torch.from_numpy(x).to(dev) for x in (qq, qd, u))
             outs = (torch.empty((n, 98), device=dev), torch.empty((n, 7), device=dev), torch.empty((n, 49), device=dev))
-            plan = ctx.plan_ragged(off, tq, tqd, tu, *outs)
-            o = [int(x) for x in off]
-            trajs = [(o[t + 1] - o[t], tq[o[t]:], tqd[o[t]:], tu[o[t]:], outs[0][o[t]:], outs[1][o[t]:],
+            o = [int(x) for x in mem_off]
+            trajs = [(int(off[t + 1] - off[t]), tq[o[t]:], tqd[o[t]:], tu[o[t]:], outs[0][o[t]:], outs[1][o[t]:],
                       outs[2][o[t]:]) for t in range(n_traj)]
+            plan = ctx.plan(trajs)
             sets.append((tq, tqd, tu, outs, plan, trajs))
     stream.synchronize()
 
@@ -313,10 +323,12 @@ def run_frg(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {
                 "workload": f"ragged mix: {n_traj} trajectories, horizons U{{{H_LO}..{H_HI}}} (seed {MIX_SEED}), "
-                            f"{n} knots per rank; batched persistent launch replayed as a CUDA graph",
+                            f"{n} knots per rank, stored in shuffled order; one persistent launch over the "
+                            f"ragged trajectory list, replayed as a CUDA graph",
                 "knots_per_step": n, "l2": f"{ROTATING_SETS} rotating input/output sets "
                                             f"({ROTATING_SETS * n * BYTES_PER_KNOT / 1e6:.0f} MB > 129 MB L2)",
-                "launch_shape": {"warps_per_cta": shape[0], "ctas_per_sm": shape[1]},
+                "launch_shape": {"plain": {"warps_per_cta": shape[0], "lanes_per_knot": ctx.lanes_per_knot()},
+                                 "persistent": "autotuned separately (frg_autotune)"},
                 "autotune_knots_per_s": tuned, "parallelism": f"replicas x{ws} (knots sharded, no collective)",
             },
             "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 84 * n, "d2h_bytes_per_step": 616 * n,

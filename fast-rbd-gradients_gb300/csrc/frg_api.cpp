@@ -60,6 +60,23 @@ bool frg_build_batch(int n_traj, const frg_traj *trajs, HostBatch &hb, std::stri
     }
     hb.segs.push_back(Segment{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, begin});
     hb.nknots = begin;
+    // contiguous: each non-empty trajectory starts where the previous one ended
+    hb.contiguous = begin > 0 && begin <= INT_MAX;
+    const frg_traj *prev = nullptr;
+    for (int t = 0; t < n_traj && hb.contiguous; t++) {
+        const frg_traj &tr = trajs[t];
+        if (tr.n_knots == 0) continue;
+        if (prev) {
+            const int64_t m = prev->n_knots;
+            hb.contiguous = tr.q == prev->q + 7 * m && tr.qd == prev->qd + 7 * m && tr.u == prev->u + 7 * m &&
+                            tr.dqdd == prev->dqdd + 98 * m && tr.qdd == prev->qdd + 7 * m &&
+                            tr.minv == prev->minv + 49 * m;
+        } else {
+            hb.whole = tr;
+        }
+        prev = &tr;
+    }
+    if (hb.contiguous) hb.whole.n_knots = begin;
     const long long ntiles = (begin + 31) / 32;
     if (ntiles > INT_MAX / 2) {
         err = "batch too large: " + std::to_string(begin) + " knots";
@@ -116,8 +133,13 @@ void DeviceBatch::release() {
 }
 
 cudaError_t frg_launch_batch(frg_ctx *ctx, const DeviceBatch &db, int nseg, int ntiles, cudaStream_t stream) {
-    return frg::launch_ragged(ctx->damping, ctx->mpc, ctx->shape, ctx->num_sms, db.segs, nseg, db.tile_seg, ntiles,
-                              db.counter, stream);
+    return frg::launch_ragged(ctx->damping, ctx->mpc, ctx->ragged_shape, ctx->num_sms, db.segs, nseg, db.tile_seg,
+                              ntiles, db.counter, stream);
+}
+
+cudaError_t frg_launch_whole(frg_ctx *ctx, const frg_traj &w, cudaStream_t stream) {
+    return frg::launch_plain(ctx->damping, ctx->mpc, ctx->shape, static_cast<int>(w.n_knots), w.q, w.qd, w.u, w.dqdd,
+                             w.qdd, w.minv, stream);
 }
 
 // ------------------------------------------------------------------ C ABI ---
@@ -186,6 +208,8 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
         !check(ctx, frg::init_group_kernels(), "latency kernel set-up") ||
         !check(ctx, frg::init_ext_kernels(), "fext / forward-dynamics kernel set-up") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream2, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !check(ctx, cudaEventCreateWithFlags(&ctx->io_fork, cudaEventDisableTiming), "cudaEventCreate") ||
         !check(ctx, cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming), "cudaEventCreate")) {
         g_orphan_error = ctx->err;
         frg_destroy(ctx);
@@ -196,6 +220,7 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
     if (opt.warps_per_cta) ctx->shape.warps_per_cta = opt.warps_per_cta;
     if (opt.ctas_per_sm) ctx->shape.ctas_per_sm = opt.ctas_per_sm;
     if (opt.lanes_per_knot) ctx->shape.lanes_per_knot = opt.lanes_per_knot;
+    ctx->ragged_shape = ctx->shape;
     *out = ctx;
     return FRG_OK;
 }
@@ -209,6 +234,11 @@ void frg_destroy(frg_ctx *ctx) {
         ctx->scratch.release();
         cudaFree(ctx->host_buf);
         if (ctx->io_stream) cudaStreamDestroy(ctx->io_stream);
+        if (ctx->io_stream2) {
+            cudaStreamSynchronize(ctx->io_stream2);
+            cudaStreamDestroy(ctx->io_stream2);
+        }
+        if (ctx->io_fork) cudaEventDestroy(ctx->io_fork);
         if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
     }
     delete ctx;
@@ -222,8 +252,8 @@ frg_status frg_set_launch_shape(frg_ctx *ctx, int warps_per_cta, int ctas_per_sm
         frg_set_error(ctx, "frg_set_launch_shape: warps_per_cta must be in [1, 8], ctas_per_sm >= 1");
         return FRG_ERR_INVALID_ARGUMENT;
     }
-    ctx->shape.warps_per_cta = warps_per_cta;
-    ctx->shape.ctas_per_sm = ctas_per_sm;
+    ctx->shape.warps_per_cta = ctx->ragged_shape.warps_per_cta = warps_per_cta;
+    ctx->shape.ctas_per_sm = ctx->ragged_shape.ctas_per_sm = ctas_per_sm;
     return FRG_OK;
 }
 
@@ -233,7 +263,7 @@ frg_status frg_set_lanes_per_knot(frg_ctx *ctx, int lanes_per_knot) {
         frg_set_error(ctx, "frg_set_lanes_per_knot: 1 (throughput mapping) or 8 (latency mapping)");
         return FRG_ERR_INVALID_ARGUMENT;
     }
-    ctx->shape.lanes_per_knot = lanes_per_knot;
+    ctx->shape.lanes_per_knot = ctx->ragged_shape.lanes_per_knot = lanes_per_knot;
     return FRG_OK;
 }
 
@@ -308,6 +338,22 @@ frg_status frg_discrete_jacobians(frg_ctx *ctx, int n_knots, const float *dqdd, 
     return FRG_OK;
 }
 
+namespace {
+
+// True if the GPU of ctx can load/store `p` directly: pinned (page-locked,
+// mapped) host memory, or device memory.
+bool device_accessible(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer == p) || a.type == cudaMemoryTypeDevice ||
+           a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
 frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
                              float *dqdd, float *qdd, float *minv) {
     if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
@@ -317,7 +363,57 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
     }
     if (n_knots == 0) return FRG_OK;
     DeviceGuard g(ctx->device);
+    cudaStream_t s = ctx->io_stream;
     const size_t n = static_cast<size_t>(n_knots);
+    // Pinned host arrays: the kernel reads q, qd, u across the host link
+    // itself, and the results leave in chunks -- chunk i's kernel writes to
+    // device staging, then its device-to-host copies run on the copy engine
+    // while chunk i + 1 computes on the other stream.  The host link (about
+    // 200 GB/s each way here) bounds this call, and the kernel hides behind it.
+    if (device_accessible(q) && device_accessible(qd) && device_accessible(u) && device_accessible(dqdd) &&
+        device_accessible(qdd) && device_accessible(minv)) {
+        const size_t need = n * (98 + 7 + 49);
+        if (need > ctx->host_buf_floats) {
+            cudaFree(ctx->host_buf);
+            ctx->host_buf = nullptr;
+            ctx->host_buf_floats = 0;
+            if (cudaMalloc(&ctx->host_buf, need * sizeof(float)) != cudaSuccess) {
+                cudaGetLastError();
+                frg_set_error(ctx, "frg_gradient_host: cudaMalloc of " + std::to_string(need * 4) + " bytes failed");
+                return FRG_ERR_OUT_OF_MEMORY;
+            }
+            ctx->host_buf_floats = need;
+        }
+        float *odqdd = ctx->host_buf, *oqdd = odqdd + 98 * n, *ominv = oqdd + 7 * n;
+        // 3 chunks of whole tiles (at least 4096 knots each): measured best
+        // between per-copy overheads and the exposed first / last chunk
+        size_t chunk = std::max<size_t>(4096, (n / 3 + 31) / 32 * 32);
+        cudaStream_t st[2] = {ctx->io_stream, ctx->io_stream2};
+        if (!check(ctx, cudaEventRecord(ctx->io_fork, st[0]), "event record") ||
+            !check(ctx, cudaStreamWaitEvent(st[1], ctx->io_fork, 0), "stream wait"))
+            return FRG_ERR_CUDA;
+        int i = 0;
+        for (size_t k0 = 0; k0 < n; k0 += chunk, i++) {
+            const size_t m = std::min(chunk, n - k0);
+            cudaStream_t sc = st[i & 1];
+            if (!check(ctx,
+                       frg::launch_plain(ctx->damping, ctx->mpc, ctx->shape, static_cast<int>(m), q + 7 * k0,
+                                         qd + 7 * k0, u + 7 * k0, odqdd + 98 * k0, oqdd + 7 * k0, ominv + 49 * k0, sc),
+                       "frg_gradient_host launch") ||
+                !check(ctx, cudaMemcpyAsync(dqdd + 98 * k0, odqdd + 98 * k0, 98 * m * sizeof(float),
+                                            cudaMemcpyDeviceToHost, sc), "D2H dqdd") ||
+                !check(ctx, cudaMemcpyAsync(qdd + 7 * k0, oqdd + 7 * k0, 7 * m * sizeof(float), cudaMemcpyDeviceToHost, sc),
+                       "D2H qdd") ||
+                !check(ctx, cudaMemcpyAsync(minv + 49 * k0, ominv + 49 * k0, 49 * m * sizeof(float),
+                                            cudaMemcpyDeviceToHost, sc), "D2H minv"))
+                return FRG_ERR_CUDA;
+        }
+        if (!check(ctx, cudaStreamSynchronize(st[1]), "frg_gradient_host sync") ||
+            !check(ctx, cudaStreamSynchronize(st[0]), "frg_gradient_host sync"))
+            return FRG_ERR_CUDA;
+        return FRG_OK;
+    }
+    // Pageable host arrays: stage through device buffers owned by ctx.
     const size_t need = n * (3 * 7 + 98 + 7 + 49);
     if (need > ctx->host_buf_floats) {
         cudaFree(ctx->host_buf);
@@ -332,7 +428,6 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
     }
     float *dq = ctx->host_buf, *dqd = dq + 7 * n, *du = dqd + 7 * n, *ddqdd = du + 7 * n, *dqdd_ = ddqdd + 98 * n,
           *dminv = dqdd_ + 7 * n;
-    cudaStream_t s = ctx->io_stream;
     const size_t b7 = 7 * n * sizeof(float);
     if (!check(ctx, cudaMemcpyAsync(dq, q, b7, cudaMemcpyHostToDevice, s), "H2D q") ||
         !check(ctx, cudaMemcpyAsync(dqd, qd, b7, cudaMemcpyHostToDevice, s), "H2D qd") ||
@@ -385,6 +480,10 @@ frg_status frg_gradient_batched(frg_ctx *ctx, int n_traj, const frg_traj *trajs,
     }
     if (hb.nknots == 0) return FRG_OK;
     DeviceGuard g(ctx->device);
+    if (hb.contiguous) {
+        if (!check(ctx, frg_launch_whole(ctx, hb.whole, stream), "batched launch")) return FRG_ERR_CUDA;
+        return FRG_OK;
+    }
     // the one-shot descriptor buffers are reused: wait for the previous user
     if (!check(ctx, cudaEventSynchronize(ctx->scratch_done), "scratch wait")) return FRG_ERR_CUDA;
     const int nseg = n_traj, ntiles = static_cast<int>(hb.tile_seg.size());

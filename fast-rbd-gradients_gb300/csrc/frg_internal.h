@@ -22,11 +22,16 @@ struct DeviceGuard {
     }
 };
 
-// Descriptor list of a batched launch, built on the host.
+// Descriptor list of a batched launch, built on the host.  When every
+// trajectory's arrays follow the previous one's in memory the batch is one
+// contiguous run of knots (`whole`) and runs on the plain kernel, without
+// per-tile descriptor lookups.
 struct HostBatch {
     std::vector<frg::Segment> segs;  // n_traj + 1 (end sentinel)
     std::vector<int> tile_seg;       // one per 32-knot tile
     long long nknots = 0;
+    bool contiguous = false;
+    frg_traj whole{};
 };
 
 // The same list on the device, plus the persistent kernel's work counter.
@@ -42,10 +47,13 @@ struct DeviceBatch {
 struct frg_ctx {
     int device = 0;
     bool damping = false, mpc = false;
-    frg::LaunchShape shape;
+    frg::LaunchShape shape;         // plain launches (contiguous knots)
+    frg::LaunchShape ragged_shape;  // persistent launches over scattered trajectories
     int num_sms = 0;
     std::string err;
     cudaStream_t io_stream = nullptr;   // frg_gradient_host
+    cudaStream_t io_stream2 = nullptr;  // second stream of its chunk pipeline
+    cudaEvent_t io_fork = nullptr;
     float *host_buf = nullptr;          // device staging for frg_gradient_host
     size_t host_buf_floats = 0;
     DeviceBatch scratch;                // frg_gradient_batched descriptors
@@ -57,12 +65,16 @@ struct frg_plan {
     DeviceBatch dev;
     int nseg = 0, ntiles = 0;
     long long nknots = 0;
+    bool contiguous = false;
+    frg_traj whole{};
     cudaGraphExec_t exec = nullptr;
 };
 
 void frg_set_error(frg_ctx *ctx, const std::string &msg);
 bool frg_build_batch(int n_traj, const frg_traj *trajs, HostBatch &hb, std::string &err);
 cudaError_t frg_launch_batch(frg_ctx *ctx, const DeviceBatch &db, int nseg, int ntiles, cudaStream_t stream);
+// Plain launch over a contiguous batch (HostBatch::whole).
+cudaError_t frg_launch_whole(frg_ctx *ctx, const frg_traj &whole, cudaStream_t stream);
 bool frg_offsets_to_trajs(int n_traj, const int64_t *offsets, const float *q, const float *qd, const float *u,
                           float *dqdd, float *qdd, float *minv, std::vector<frg_traj> &out);
 

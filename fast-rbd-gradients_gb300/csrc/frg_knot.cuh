@@ -460,6 +460,24 @@ __device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const floa
 
 // One column of d tau / dq (QSIDE) or d tau / dqd for the differentiated joint c
 // (compute_vafdu :787-829 and compute_cdu :832-857 restricted to column c).
+// df_k = I_k da + dv x* (I_k v_k) + v_k x* (I_k dv): the force tangent of
+// link k from its velocity / acceleration tangents (dv, da).
+template <int k>
+__device__ __forceinline__ void link_force_tangent(float df[6], const float v[6], const float Iv[6],
+                                                   const float dv[6], const float da[6]) {
+    float Idv[6];
+    imul<k>(Idv, dv);
+    imul<k>(df, da);
+    crf_acc(df, dv, Iv);
+    crf_acc(df, v, Idv);
+}
+
+// One column of d tau / dq (QSIDE) or d tau / dqd for the differentiated joint c
+// (compute_vafdu :787-829 and compute_cdu :832-857 restricted to column c).
+// The forward sweep is software-pipelined: the block of link k computes the
+// force tangent of link k - 1 together with the velocity / acceleration
+// tangents of link k, two independent dependency chains in one basic block
+// (the link loop is unrolled, the column c is a warp-uniform runtime value).
 template <bool QSIDE, bool DAMP>
 __device__ __forceinline__ void dtau_column(const WarpSmem *ws, int lane, int c, const float qd[7],
                                             const float sq[7], const float cq[7], float dtau[7]) {
@@ -467,48 +485,49 @@ __device__ __forceinline__ void dtau_column(const WarpSmem *ws, int lane, int c,
     float dv[6], da[6];
     static_for<0, kJoints>([&](auto K) {
         constexpr int k = decltype(K)::value;
-        if (k >= c) {
+        if (k == c) {
             float v[6], Iv[6];
             lds_link(ws, k, lane, v, Iv);
-            float ndv[6], nda[6], Idv[6];
-            if (k == c) {
-                if constexpr (QSIDE) {
-                    // dv = crm(X_k v_{k-1}) S; (X_k v_{k-1}) and v_k agree outside entry 2
-                    ndv[0] = v[1]; ndv[1] = -v[0]; ndv[2] = 0.0f;
-                    ndv[3] = v[4]; ndv[4] = -v[3]; ndv[5] = 0.0f;
-                    // da = crm(dv) S qd_k + crm(X_k a_{k-1}) S
-                    const float4 xa = ws->link[kSlotsPerLink * k + 3][lane];  // (Xa0, Xa1, Xa3, Xa4)
-                    nda[0] = fmaf(ndv[1], qd[k], xa.y);
-                    nda[1] = fmaf(-ndv[0], qd[k], -xa.x);
-                    nda[2] = 0.0f;
-                    nda[3] = fmaf(ndv[4], qd[k], xa.w);
-                    nda[4] = fmaf(-ndv[3], qd[k], -xa.z);
-                    nda[5] = 0.0f;
-                    imul<k>(Idv, ndv);
-                } else {
-                    // dv = S, da = crm(v_k) S, I dv = I_k[:,2]
-                    ndv[0] = ndv[1] = 0.0f; ndv[2] = 1.0f; ndv[3] = ndv[4] = ndv[5] = 0.0f;
-                    nda[0] = v[1]; nda[1] = -v[0]; nda[2] = 0.0f;
-                    nda[3] = v[4]; nda[4] = -v[3]; nda[5] = 0.0f;
-                    icol2<k>(Idv);
-                }
+            if constexpr (QSIDE) {
+                // dv = crm(X_k v_{k-1}) S; (X_k v_{k-1}) and v_k agree outside entry 2
+                dv[0] = v[1]; dv[1] = -v[0]; dv[2] = 0.0f;
+                dv[3] = v[4]; dv[4] = -v[3]; dv[5] = 0.0f;
+                // da = crm(dv) S qd_k + crm(X_k a_{k-1}) S
+                const float4 xa = ws->link[kSlotsPerLink * k + 3][lane];  // (Xa0, Xa1, Xa3, Xa4)
+                da[0] = fmaf(dv[1], qd[k], xa.y);
+                da[1] = fmaf(-dv[0], qd[k], -xa.x);
+                da[2] = 0.0f;
+                da[3] = fmaf(dv[4], qd[k], xa.w);
+                da[4] = fmaf(-dv[3], qd[k], -xa.z);
+                da[5] = 0.0f;
             } else {
+                // dv = S, da = crm(v_k) S
+                dv[0] = dv[1] = 0.0f; dv[2] = 1.0f; dv[3] = dv[4] = dv[5] = 0.0f;
+                da[0] = v[1]; da[1] = -v[0]; da[2] = 0.0f;
+                da[3] = v[4]; da[4] = -v[3]; da[5] = 0.0f;
+            }
+        } else if (k > c) {
+            if constexpr (k >= 1) {
+                float v[6], Iv[6];
+                lds_link(ws, k - 1, lane, v, Iv);
+                link_force_tangent<k - 1>(df[k - 1], v, Iv, dv, da);
+                float ndv[6], nda[6];
                 xmotion<k>(ndv, dv, cq[k], sq[k]);
                 xmotion<k>(nda, da, cq[k], sq[k]);
                 nda[0] = fmaf(ndv[1], qd[k], nda[0]);
                 nda[1] = fmaf(-ndv[0], qd[k], nda[1]);
                 nda[3] = fmaf(ndv[4], qd[k], nda[3]);
                 nda[4] = fmaf(-ndv[3], qd[k], nda[4]);
-                imul<k>(Idv, ndv);
-            }
-            // df = I da + dv x* (I v) + v x* (I dv)
-            imul<k>(df[k], nda);
-            crf_acc(df[k], ndv, Iv);
-            crf_acc(df[k], v, Idv);
 #pragma unroll
-            for (int i = 0; i < 6; i++) { dv[i] = ndv[i]; da[i] = nda[i]; }
+                for (int i = 0; i < 6; i++) { dv[i] = ndv[i]; da[i] = nda[i]; }
+            }
         }
     });
+    {
+        float v[6], Iv[6];
+        lds_link(ws, kJoints - 1, lane, v, Iv);
+        link_force_tangent<kJoints - 1>(df[kJoints - 1], v, Iv, dv, da);
+    }
     float dF[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     static_for_down<kJoints - 1, 0>([&](auto K) {
         constexpr int k = decltype(K)::value;
@@ -577,7 +596,9 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
 
     float sq[7], cq[7], Mi[7][7], qdd[7];
     phase1<DAMP, MPC, FEXT>(ws, lane, q, qd, u, sq, cq, Mi, qdd, fx);
-    if constexpr (!FDONLY) rnea_with_qdd<MPC, FEXT>(ws, lane, qd, qdd, sq, cq, fx);
+    // with FEXT the second RNEA runs while the forces are still staged;
+    // otherwise after the Minv / qdd stores (fewer live registers)
+    if constexpr (FEXT && !FDONLY) rnea_with_qdd<MPC, FEXT>(ws, lane, qd, qdd, sq, cq, fx);
     __syncwarp();
 
     // Minv (dense) and qdd out
@@ -592,6 +613,10 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     scatter_out<7>(ws->stage, kp.qdd, lane);
     if constexpr (MIRROR) scatter_out<7>(ws->stage, mr.qdd, lane);
     if constexpr (FDONLY) return;
+    if constexpr (!FEXT) {
+        rnea_with_qdd<MPC>(ws, lane, qd, qdd, sq, cq);
+        __syncwarp();
+    }
 
     // d qdd / dq: columns 0..6 (column 0 is identically zero for this model:
     // the base joint axis is parallel to gravity, as dynamicsGradient.h:797-813 uses)

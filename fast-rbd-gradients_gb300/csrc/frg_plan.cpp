@@ -29,7 +29,8 @@ bool capture(frg_plan *plan) {
     bool good = ok(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     cudaGraph_t graph = nullptr;
     if (good) {
-        cudaError_t le = frg_launch_batch(ctx, plan->dev, plan->nseg, plan->ntiles, cs);
+        cudaError_t le = plan->contiguous ? frg_launch_whole(ctx, plan->whole, cs)
+                                          : frg_launch_batch(ctx, plan->dev, plan->nseg, plan->ntiles, cs);
         cudaError_t ee = cudaStreamEndCapture(cs, &graph);
         good = ok(ctx, le, "batched launch capture") && ok(ctx, ee, "cudaStreamEndCapture");
     }
@@ -62,11 +63,21 @@ frg_status frg_plan_create(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_
     plan->nseg = n_traj;
     plan->ntiles = static_cast<int>(hb.tile_seg.size());
     plan->nknots = hb.nknots;
+    plan->contiguous = hb.contiguous;
+    plan->whole = hb.whole;
     if (plan->nknots == 0) {
         *out = plan;
         return FRG_OK;
     }
     DeviceGuard g(ctx->device);
+    if (plan->contiguous) {  // one plain launch: no descriptor lists on the device
+        if (!capture(plan)) {
+            frg_plan_destroy(plan);
+            return FRG_ERR_CUDA;
+        }
+        *out = plan;
+        return FRG_OK;
+    }
     if (!plan->dev.reserve(plan->nseg + 1, plan->ntiles, err)) {
         cudaGetLastError();
         frg_set_error(ctx, "frg_plan_create: " + err);
@@ -136,49 +147,77 @@ frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s)
         return FRG_ERR_OUT_OF_MEMORY;
     }
     frg_traj tr{n_knots, d, d + 7 * n, d + 14 * n, d + 21 * n, d + 119 * n, d + 126 * n};
-    HostBatch hb;
     std::string err;
-    DeviceBatch db;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaStream_t s = ctx->io_stream;
     bool good = ok(ctx, cudaMemcpy(d, h.data(), sizeof(float) * 21 * n, cudaMemcpyHostToDevice), "autotune upload") &&
-                frg_build_batch(1, &tr, hb, err) && db.reserve(2, static_cast<int>(hb.tile_seg.size()), err) &&
-                ok(ctx, cudaMemcpy(db.segs, hb.segs.data(), sizeof(frg::Segment) * 2, cudaMemcpyHostToDevice), "upload") &&
-                ok(ctx, cudaMemcpy(db.tile_seg, hb.tile_seg.data(), sizeof(int) * hb.tile_seg.size(), cudaMemcpyHostToDevice),
-                   "upload") &&
                 ok(ctx, cudaEventCreate(&e0), "cudaEventCreate") && ok(ctx, cudaEventCreate(&e1), "cudaEventCreate");
-    const frg::LaunchShape saved = ctx->shape;
+    const frg::LaunchShape saved = ctx->shape, saved_r = ctx->ragged_shape;
+    auto time_ms = [&](auto launch) {
+        float ms_min = FLT_MAX;
+        for (int rep = 0; rep < 5 && good; rep++) {
+            good = ok(ctx, cudaEventRecord(e0, s), "record") && ok(ctx, launch(), "autotune launch") &&
+                   ok(ctx, cudaEventRecord(e1, s), "record") && ok(ctx, cudaEventSynchronize(e1), "sync");
+            float ms = 0;
+            if (good && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) ms_min = std::min(ms_min, ms);
+        }
+        return ms_min;
+    };
+    // 1) contiguous batches: the plain kernel (threads per knot x warps per CTA)
     frg::LaunchShape best = saved;
     float best_ms = FLT_MAX;
-    const int ntiles = static_cast<int>(hb.tile_seg.size());
     for (int lanes : {1, 8})
-    for (int w : {1, 2, 3, 4, 6, 8}) {
-        if (!good) break;
-        const int occ = frg::max_ctas_per_sm(w, lanes);
-        if (occ < 1) continue;
-        for (int c : {occ, std::max(1, occ / 2)}) {
+        for (int w : {1, 2, 3, 4, 6, 8}) {
+            if (!good) break;
             ctx->shape.warps_per_cta = w;
-            ctx->shape.ctas_per_sm = c;
             ctx->shape.lanes_per_knot = lanes;
-            float ms_min = FLT_MAX;
-            for (int rep = 0; rep < 5 && good; rep++) {
-                good = ok(ctx, cudaEventRecord(e0, s), "record") &&
-                       ok(ctx, frg_launch_batch(ctx, db, 1, ntiles, s), "autotune launch") &&
-                       ok(ctx, cudaEventRecord(e1, s), "record") && ok(ctx, cudaEventSynchronize(e1), "sync");
-                float ms = 0;
-                if (good && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) ms_min = std::min(ms_min, ms);
-            }
-            if (ms_min < best_ms) {
-                best_ms = ms_min;
+            const float ms = time_ms([&] { return frg_launch_whole(ctx, tr, s); });
+            if (ms < best_ms) {
+                best_ms = ms;
                 best = ctx->shape;
             }
         }
+    // 2) scattered trajectories: the persistent kernel (x resident CTAs per SM),
+    //    on the same knots cut into 128-knot trajectories in reversed order
+    std::vector<frg_traj> scattered;
+    for (size_t k0 = 0; k0 < n; k0 += 128) {
+        const size_t m = std::min<size_t>(128, n - k0);
+        scattered.push_back(frg_traj{static_cast<int64_t>(m), d + 7 * k0, d + 7 * n + 7 * k0, d + 14 * n + 7 * k0,
+                                     d + 21 * n + 98 * k0, d + 119 * n + 7 * k0, d + 126 * n + 49 * k0});
     }
+    std::reverse(scattered.begin(), scattered.end());
+    HostBatch hs;
+    DeviceBatch ds;
+    good = good && frg_build_batch(static_cast<int>(scattered.size()), scattered.data(), hs, err) &&
+           ds.reserve(static_cast<int>(hs.segs.size()), static_cast<int>(hs.tile_seg.size()), err) &&
+           ok(ctx, cudaMemcpy(ds.segs, hs.segs.data(), sizeof(frg::Segment) * hs.segs.size(), cudaMemcpyHostToDevice),
+              "upload") &&
+           ok(ctx, cudaMemcpy(ds.tile_seg, hs.tile_seg.data(), sizeof(int) * hs.tile_seg.size(), cudaMemcpyHostToDevice),
+              "upload");
+    frg::LaunchShape best_r = saved_r;
+    float best_r_ms = FLT_MAX;
+    const int nseg = static_cast<int>(scattered.size()), ntiles_s = static_cast<int>(hs.tile_seg.size());
+    for (int lanes : {1, 8})
+        for (int w : {1, 2, 3, 4, 6, 8}) {
+            if (!good) break;
+            const int occ = frg::max_ctas_per_sm(w, lanes);
+            for (int c = occ; c >= 1; c--) {  // every residency: fewer CTAs can balance the last wave
+                ctx->ragged_shape.warps_per_cta = w;
+                ctx->ragged_shape.ctas_per_sm = c;
+                ctx->ragged_shape.lanes_per_knot = lanes;
+                const float ms = time_ms([&] { return frg_launch_batch(ctx, ds, nseg, ntiles_s, s); });
+                if (ms < best_r_ms) {
+                    best_r_ms = ms;
+                    best_r = ctx->ragged_shape;
+                }
+            }
+        }
+    ds.release();
     if (!good && err.size()) frg_set_error(ctx, "frg_autotune: " + err);
     ctx->shape = good ? best : saved;
+    ctx->ragged_shape = good ? best_r : saved_r;
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    db.release();
     cudaFree(d);
     if (!good) return FRG_ERR_CUDA;
     if (best_knots_per_s) *best_knots_per_s = best_ms < FLT_MAX ? static_cast<double>(n_knots) / (best_ms * 1e-3) : 0.0;

@@ -372,7 +372,7 @@ frg_status frg_server_create(frg_ctx *ctx, const frg_server_options *opt_in, frg
     if (!s) return FRG_ERR_OUT_OF_MEMORY;
     s->ctx = ctx;
     s->opt = opt;
-    s->shape = ctx->shape;
+    s->shape = ctx->ragged_shape;
     if (opt.warps_per_cta) s->shape.warps_per_cta = opt.warps_per_cta;
     if (opt.ctas_per_sm) s->shape.ctas_per_sm = opt.ctas_per_sm;
     if (s->shape.lanes_per_knot == 8) s->shape.lanes_per_knot = 1;  // big batches: throughput mapping

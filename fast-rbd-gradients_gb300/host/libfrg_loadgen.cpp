@@ -147,8 +147,11 @@ extern "C" int frg_loadgen_run(frg_server *srv, const frg_loadgen_cfg *cfg, frg_
                         start_session(rng);
                         next_arrival += gap(rng);
                     }
-                else
-                    while (active < static_cast<uint64_t>(cfg->concurrency) && started < limit) start_session(rng);
+                else {  // top up to `concurrency` once per pass, so the clock is re-read
+                    const uint64_t have = active.load();
+                    const uint64_t want = have < static_cast<uint64_t>(cfg->concurrency) ? cfg->concurrency - have : 0;
+                    for (uint64_t i = 0; i < want && started < limit; i++) start_session(rng);
+                }
             }
             if (!window_open && active == 0) break;
             frg_request_info info;

@@ -86,7 +86,8 @@ void frg_destroy(frg_ctx *ctx);
 /* Message of the last failed call on ctx ("" if none).  ctx may be NULL. */
 const char *frg_last_error(const frg_ctx *ctx);
 
-/* Launch shape used by every launch of ctx (the autotuner sets it too). */
+/* Launch shape of ctx's launches (sets both the plain and the persistent
+ * shape; the autotuner tunes them separately and get returns the plain one). */
 frg_status frg_set_launch_shape(frg_ctx *ctx, int warps_per_cta, int ctas_per_sm);
 frg_status frg_get_launch_shape(const frg_ctx *ctx, int *warps_per_cta, int *ctas_per_sm);
 /* Threads per knot of every launch of ctx: 1 or 8 (the autotuner sets it too). */
@@ -103,10 +104,12 @@ frg_status frg_gradient(frg_ctx *ctx, int n_knots, const float *q, const float *
                         float *qdd, float *minv, frg_stream stream);
 
 /*
- * Same, for HOST arrays: copies the inputs in, runs, copies the outputs back
- * through device buffers owned by ctx, and returns when the results are in
- * the host arrays (the time_GPU.cu:313-316 "Compute + I/O" sequence).  Host
- * arrays from frg_host_alloc() (pinned) copy fastest.
+ * Same, for HOST arrays, synchronous: returns when the results are in the host
+ * arrays (the time_GPU.cu:313-316 "Compute + I/O" sequence).  Pinned arrays
+ * (frg_host_alloc, cudaHostAlloc / cudaHostRegister) take a pipelined path:
+ * the kernel reads the inputs across the host link itself and the results are
+ * copied back in chunks that overlap the next chunk's arithmetic; pageable
+ * arrays are staged through device buffers owned by ctx.
  */
 frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
                              float *dqdd, float *qdd, float *minv);
@@ -147,8 +150,11 @@ typedef struct frg_traj {
 frg_status frg_gradient_per_trajectory(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_stream stream);
 
 /*
- * Batched form: ONE persistent launch that walks the 32-knot tiles of all
- * trajectories' knots (a ragged offset list), asynchronous on `stream`.
+ * Batched form: ONE launch over all trajectories' knots, asynchronous on
+ * `stream`.  Trajectories scattered in memory run on a persistent kernel that
+ * walks the 32-knot tiles of the ragged list; trajectories that lie back to
+ * back in memory (e.g. offsets into concatenated arrays) are one contiguous
+ * run of knots and take the plain kernel, without per-tile lookups.
  * Builds the launch's descriptor list on every call; for a batch that is run
  * repeatedly, build an frg_plan once instead.
  */
@@ -194,9 +200,10 @@ int64_t frg_plan_knots(const frg_plan *plan);
 void frg_plan_destroy(frg_plan *plan);
 
 /*
- * Autotuner: times every launch shape (threads per knot x warps per CTA x
- * resident CTAs per SM) on n_knots synthetic knots with CUDA events and keeps
- * the fastest in ctx.
+ * Autotuner: on n_knots synthetic knots, times with CUDA events every shape of
+ * the plain kernel (threads per knot x warps per CTA; contiguous batches) and
+ * of the persistent kernel (x resident CTAs per SM; trajectories scattered in
+ * memory) and keeps the fastest of each in ctx.
  * Writes the best throughput (knots/s) if best_knots_per_s is not NULL.
  */
 frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s);

@@ -138,3 +138,27 @@ def test_latency_mapping_parity(golden, damping, mpc, n):
         assert max_err(x, y) <= 1e-5
     tag = f"f64_d{damping}_m{mpc}"
     assert max_err(g[0], golden[f"dqdd_{tag}"]) <= TOL and max_err(g[2], golden[f"minv_{tag}"]) <= TOL
+
+
+def test_host_call_pinned_zero_copy_equals_staged():
+    """frg_gradient_host on pinned buffers (kernel reads/writes host memory
+    directly) gives the same bits as on pageable buffers (staged copies)."""
+    import ctypes
+    n = 3000
+    q, qd, u = frg.sample_knots(n, seed=31)
+    L = frg.lib()
+    bufs = {}
+    for name, w in (("q", 7), ("qd", 7), ("u", 7), ("dqdd", 98), ("qdd", 7), ("minv", 49)):
+        ptr = L.frg_host_alloc(4 * w * n)
+        assert ptr
+        bufs[name] = (ptr, np.ctypeslib.as_array((ctypes.c_float * (w * n)).from_address(ptr)).reshape(n, w))
+    try:
+        bufs["q"][1][:], bufs["qd"][1][:], bufs["u"][1][:] = q, qd, u
+        with frg.Context() as ctx:
+            staged = ctx.gradient_host(q, qd, u)
+            ctx.gradient_host_into(n, *(bufs[k][0] for k in ("q", "qd", "u", "dqdd", "qdd", "minv")))
+        for name, ref in zip(("dqdd", "qdd", "minv"), staged):
+            assert np.array_equal(bufs[name][1], ref)
+    finally:
+        for ptr, _ in bufs.values():
+            L.frg_host_free(ptr)
