@@ -1,7 +1,7 @@
 """Benchmark: iiwa_14 forward-dynamics gradients on GB300.
 
 Workload (one "step"): the ragged 512-trajectory mix -- horizons ~ U{8..256}
-(seed 2021, 67.6k knots), knots q ~ U(URDF joint limits), qd ~ U(-2, 2),
+(seed 2021, 66,809 knots), knots q ~ U(URDF joint limits), qd ~ U(-2, 2),
 u ~ U(-20, 20) (seeded synthetic data; the reference ships no dataset) --
 through the full path (RNEA, Minv, q̈, dtau/dq, dtau/dqd, -Minv dtau) in FP32.
 
@@ -12,7 +12,14 @@ through the full path (RNEA, Minv, q̈, dtau/dq, dtau/dqd, -Minv dtau) in FP32.
             (frg_gradient_host): H2D of q, qd, u from pinned memory, kernel,
             D2H of dqdd, qdd, Minv inside every timed step.
   plain     the plain form of the same mix: one launch per trajectory.
-  served    p50/p99 request latency of the continuous-batching server.
+  plain_scaling  one plain launch per batch of N contiguous knots, N in
+            {16, 32, 64, 128, 1024, 65536}, the faster thread mapping kept.
+  served    p50/p99 request latency of the continuous-batching server, and
+            the 2 GiB-pool admission run with 1 % of its calls verified by
+            the FP64 GPU build.
+  parity    max per-knot Frobenius-relative error of dqdd, qdd, Minv over
+            every knot the timed launches produced, against the FP64 GPU
+            build (frg_verify_f64).
   roofline  dominant kernel (the batched kernel): algorithmic bytes
             (84 B in + 616 B out per knot) / CUDA-event launch time vs the
             measured HBM copy peak; FP32 work at the reference's 35,257
@@ -57,6 +64,10 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving latency measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-traj", type=int, default=N_TRAJ, help="trajectories in the ragged mix")
+    ap.add_argument("--plain-n", type=int, default=0,
+                    help="with --profile: time plain launches of this many contiguous knots instead of the mix")
+    ap.add_argument("--plain-lanes", type=int, default=1, choices=(1, 8),
+                    help="with --plain-n: threads per knot of those launches")
     ap.add_argument("--profile", action="store_true",
                     help="batched launches only (no autotune, plain form, e2e, serving or CPU baseline): "
                          "the command the ncu summaries in profiles/ capture")
@@ -150,6 +161,57 @@ class ClockSampler:
         return out
 
 
+PLAIN_SIZES = (16, 32, 64, 128, 1024, 65536)
+
+
+def plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak, steps=20):
+    """Plain path, one launch per batch of N contiguous device-resident knots
+    (BASELINE's scaling config), in both thread mappings; the faster is kept."""
+    import frg
+    out = []
+    q, qd, u = frg.sample_knots(max(PLAIN_SIZES), seed=99)
+    tq, tqd, tu = (torch.from_numpy(x).to(dev) for x in (q, qd, u))
+    o = [torch.empty((max(PLAIN_SIZES), w), device=dev) for w in (98, 7, 49)]
+    saved = ctx.lanes_per_knot()
+    for n in PLAIN_SIZES:
+        best = None
+        for lanes in (1, 8):
+            ctx.set_lanes_per_knot(lanes)
+            for _ in range(3):
+                ctx.gradient(n, tq, tqd, tu, *o, stream=stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                ctx.gradient(n, tq, tqd, tu, *o, stream=stream)
+            e1.record(stream)
+            stream.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            if best is None or ms < best[0]:
+                best = (ms, lanes)
+        ms, lanes = best
+        out.append({"n": n, "us_per_launch": round(ms * 1e3, 2), "knots_per_s": n / (ms * 1e-3),
+                    "lanes_per_knot": lanes,
+                    "hbm_frac": BYTES_PER_KNOT * n / (ms * 1e-3) / 1e9 / float(peaks["hbm_gbs"]),
+                    "fp32_frac": FLOP_PER_KNOT_REF * n / (ms * 1e-3) / 1e12 / fp32_peak})
+    ctx.set_lanes_per_knot(saved)
+    return out
+
+
+def mix_parity(ctx, torch, sets, n, stream):
+    """Max per-knot Frobenius-relative error of each output matrix over the
+    results of the batched launches, against the FP64 GPU build."""
+    err = torch.empty((n, 3), dtype=torch.float64, device=sets[0][0].device)
+    worst = torch.zeros(3, dtype=torch.float64, device=err.device)
+    with torch.cuda.stream(stream):
+        for tq, tqd, tu, outs, _, _ in sets:
+            ctx.verify_f64(n, tq, tqd, tu, *outs, err, stream=stream)
+            worst = torch.maximum(worst, err.max(dim=0).values)
+    stream.synchronize()
+    w = worst.cpu().tolist()
+    return {"max_frob_rel_dqdd": w[0], "max_frob_rel_qdd": w[1], "max_frob_rel_minv": w[2], "bar": 1e-4,
+            "knots": n * len(sets), "checked_by": "FP64 GPU verification build (frg_verify_f64), every knot"}
+
+
 def cpu_baseline(q, qd, u, budget_s=8.0):
     """The oracle port (C restatement of the reference CPU path) on all host
     threads, on a bounded sample of the workload's knots."""
@@ -207,6 +269,17 @@ def run_frg(args):
     peaks, peaks_src = load_peaks()
 
     ctx = frg.Context(device=dev.index)
+    if args.profile and args.plain_n:
+        pn = args.plain_n
+        pq, pqd, pu = (torch.from_numpy(x).to(dev) for x in frg.sample_knots(pn, seed=99))
+        po = [torch.empty((pn, w), device=dev) for w in (98, 7, 49)]
+        ctx.set_lanes_per_knot(args.plain_lanes)
+        for _ in range(args.warmup + args.steps):
+            ctx.gradient(pn, pq, pqd, pu, *po)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": True, "plain_n": pn, "lanes_per_knot": args.plain_lanes}))
+        ctx.close()
+        return 0
     tuned = None if args.profile else ctx.autotune(n)
     shape = ctx.launch_shape()
 
@@ -270,6 +343,10 @@ def run_frg(args):
     value, total_ms, _ = fdist.aggregate(sum(step_ms), n, args.steps, device=dev)
     ms_per_step = total_ms / args.steps
 
+    # ---- parity of the timed launches' results: every knot of every rotating
+    # set against the FP64 GPU verification build ----
+    parity = None if args.profile else mix_parity(ctx, torch, sets, n, stream)
+
     if args.profile:
         if rank == 0:
             print(json.dumps({"profile": True, "knots_per_step": n, "steps": args.steps,
@@ -300,13 +377,17 @@ def run_frg(args):
     for p in [hq, hqd, hu] + hout:
         frg.lib().frg_host_free(p)
 
+    # ---- plain path scaling (one launch per batch of N knots) ----
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = torch.cuda.get_device_properties(dev).multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+    scaling = plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak)
+
     # ---- serving: latency at 50 % of saturation, and admission under a 2 GiB pool ----
     served = served_adm = None
     if not args.no_serve:
-        import frg_oracle
         from frg import serve
         served = serve.bench_latency(ctx, seconds=3.0)
-        served_adm = serve.bench_admission(ctx, oracle=frg_oracle)
+        served_adm = serve.bench_admission(ctx)
 
     line = None
     if rank == 0:
@@ -336,6 +417,8 @@ def run_frg(args):
             "plain_per_trajectory": {"value": plain_value, "unit": UNIT, "launches_per_step": n_traj,
                                      "ms_per_step": statistics.mean(plain_ms)},
             "batched_vs_plain": value / ws / plain_value,
+            "plain_scaling": scaling,
+            "parity": parity,
             "served": served,
             "served_admission": served_adm,
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",

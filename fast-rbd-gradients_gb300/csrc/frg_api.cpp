@@ -207,6 +207,7 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
         !check(ctx, frg::init_kernels(), "kernel set-up") ||
         !check(ctx, frg::init_group_kernels(), "latency kernel set-up") ||
         !check(ctx, frg::init_ext_kernels(), "fext / forward-dynamics kernel set-up") ||
+        !check(ctx, frg::init_f64_kernels(), "FP64 kernel set-up") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream2, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !check(ctx, cudaEventCreateWithFlags(&ctx->io_fork, cudaEventDisableTiming), "cudaEventCreate") ||
@@ -233,6 +234,7 @@ void frg_destroy(frg_ctx *ctx) {
         if (ctx->scratch_done) cudaEventSynchronize(ctx->scratch_done);
         ctx->scratch.release();
         cudaFree(ctx->host_buf);
+        cudaFree(ctx->f64_buf);
         if (ctx->io_stream) cudaStreamDestroy(ctx->io_stream);
         if (ctx->io_stream2) {
             cudaStreamSynchronize(ctx->io_stream2);
@@ -338,6 +340,57 @@ frg_status frg_discrete_jacobians(frg_ctx *ctx, int n_knots, const float *dqdd, 
     return FRG_OK;
 }
 
+frg_status frg_gradient_f64(frg_ctx *ctx, int n_knots, const double *q, const double *qd, const double *u,
+                            double *dqdd, double *qdd, double *minv, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 0 || (n_knots > 0 && !(q && qd && u && dqdd && qdd && minv))) {
+        frg_set_error(ctx, "frg_gradient_f64: negative n_knots or null pointer");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n_knots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    if (!check(ctx, frg::launch_plain_f64(ctx->damping, ctx->mpc, ctx->num_sms, n_knots, q, qd, u, dqdd, qdd, minv,
+                                          stream),
+               "frg_gradient_f64 launch"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+frg_status frg_verify_f64(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                          const float *dqdd, const float *qdd, const float *minv, double *err, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 0 || (n_knots > 0 && !(q && qd && u && dqdd && qdd && minv && err))) {
+        frg_set_error(ctx, "frg_verify_f64: negative n_knots or null pointer");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n_knots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    const size_t n = static_cast<size_t>(n_knots), need = 175 * n;
+    if (ctx->f64_buf_doubles < need) {
+        cudaFree(ctx->f64_buf);  // waits for earlier work that may still read it
+        ctx->f64_buf = nullptr;
+        ctx->f64_buf_doubles = 0;
+        if (cudaMalloc(&ctx->f64_buf, sizeof(double) * need) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->f64_buf = nullptr;
+            frg_set_error(ctx, "frg_verify_f64: out of device memory for the FP64 scratch");
+            return FRG_ERR_OUT_OF_MEMORY;
+        }
+        ctx->f64_buf_doubles = need;
+    }
+    double *b = ctx->f64_buf;
+    double *q64 = b, *qd64 = b + 7 * n, *u64 = b + 14 * n;
+    double *dqdd64 = b + 21 * n, *qdd64 = b + 119 * n, *minv64 = b + 126 * n;
+    if (!check(ctx, frg::launch_widen_inputs(ctx->num_sms, n_knots, q, qd, u, b, stream), "frg_verify_f64 widen") ||
+        !check(ctx, frg::launch_plain_f64(ctx->damping, ctx->mpc, ctx->num_sms, n_knots, q64, qd64, u64, dqdd64,
+                                          qdd64, minv64, stream),
+               "frg_verify_f64 launch") ||
+        !check(ctx, frg::launch_compare_f64(ctx->num_sms, n_knots, dqdd, qdd, minv, dqdd64, qdd64, minv64, err, stream),
+               "frg_verify_f64 compare"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
 namespace {
 
 // True if the GPU of ctx can load/store `p` directly: pinned (page-locked,
@@ -375,6 +428,7 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
         const size_t need = n * (98 + 7 + 49);
         if (need > ctx->host_buf_floats) {
             cudaFree(ctx->host_buf);
+        cudaFree(ctx->f64_buf);
             ctx->host_buf = nullptr;
             ctx->host_buf_floats = 0;
             if (cudaMalloc(&ctx->host_buf, need * sizeof(float)) != cudaSuccess) {
@@ -417,6 +471,7 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
     const size_t need = n * (3 * 7 + 98 + 7 + 49);
     if (need > ctx->host_buf_floats) {
         cudaFree(ctx->host_buf);
+        cudaFree(ctx->f64_buf);
         ctx->host_buf = nullptr;
         ctx->host_buf_floats = 0;
         if (cudaMalloc(&ctx->host_buf, need * sizeof(float)) != cudaSuccess) {

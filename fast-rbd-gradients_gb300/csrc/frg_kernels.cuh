@@ -80,4 +80,18 @@ cudaError_t launch_ext(bool damping, bool mpc, const LaunchShape &shape, int n, 
 cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float dt, float *A, float *B,
                               cudaStream_t stream);
 
+// FP64 verification build (frg_f64_kernels.cu): the plain path in double, and
+// the two helpers of the sampled check of FP32 results (float inputs widened to
+// out [3][n][7]; per-knot Frobenius-relative errors err [n][3] of FP32 dqdd,
+// qdd, minv against FP64 results).
+cudaError_t init_f64_kernels();
+size_t f64_warp_smem_bytes();
+cudaError_t launch_plain_f64(bool damping, bool mpc, int num_sms, long long n, const double *q, const double *qd,
+                             const double *u, double *dqdd, double *qdd, double *minv, cudaStream_t stream);
+cudaError_t launch_widen_inputs(int num_sms, long long n, const float *q, const float *qd, const float *u,
+                                double *out, cudaStream_t stream);
+cudaError_t launch_compare_f64(int num_sms, long long n, const float *dqdd, const float *qdd, const float *minv,
+                               const double *rdqdd, const double *rqdd, const double *rminv, double *err,
+                               cudaStream_t stream);
+
 }  // namespace frg

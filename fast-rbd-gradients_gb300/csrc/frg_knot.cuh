@@ -16,33 +16,54 @@
 #pragma once
 #include "frg_model.cuh"
 
-namespace frg {
+namespace FRG_NS {
 
-// Per-link data that the tangent sweeps re-read, as float4 slots:
+// Per-link data that the tangent sweeps re-read, as real4 slots:
 //   0: v[0..3]   1: v[4..5] Iv[0..1]   2: Iv[2..5]   3: (X a_{k-1})[0,1,3,4]
 //   4: f_k[0,1,3,4] after the backward pass
 constexpr int kSlotsPerLink = 5;
 constexpr int kLinkSlots = kSlotsPerLink * kJoints;
 constexpr int kStageFloats = 49;  // per lane
 
+// Four reals as one 16-byte-aligned shared-memory slot.
+template <typename T> struct Real4Of;
+template <> struct Real4Of<float> { using type = float4; };
+struct alignas(16) double4x { double x, y, z, w; };
+template <> struct Real4Of<double> { using type = double4x; };
+using real4 = Real4Of<real>::type;
+__device__ __forceinline__ real4 make_real4(real a, real b, real c, real d) {
+    real4 v;
+    v.x = a; v.y = b; v.z = c; v.w = d;
+    return v;
+}
+// Read-only 16-byte loads of one slot.
+__device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
+__device__ __forceinline__ double4x ldg4(const double4x *p) {
+    const double2 *d = reinterpret_cast<const double2 *>(p);
+    const double2 a = __ldg(d), b = __ldg(d + 1);
+    double4x v;
+    v.x = a.x; v.y = a.y; v.z = b.x; v.w = b.y;
+    return v;
+}
+
 struct WarpSmem {
-    float4 link[kLinkSlots][32];
-    float stage[32 * kStageFloats];
+    real4 link[kLinkSlots][32];
+    real stage[32 * kStageFloats];
 };
 
 // A lane's knot: input and output bases (q == nullptr: idle lane).
 struct KnotPtrs {
-    const float *q, *qd, *u;
-    float *dqdd, *qdd, *minv;
-    const float *fext = nullptr;  // [7][6] external spatial force per link (link frame), optional
+    const real *q, *qd, *u;
+    real *dqdd, *qdd, *minv;
+    const real *fext = nullptr;  // [7][6] external spatial force per link (link frame), optional
 };
 
-__device__ __forceinline__ const float *shfl_ptr(const float *p, int src) {
-    return reinterpret_cast<const float *>(
+__device__ __forceinline__ const real *shfl_ptr(const real *p, int src) {
+    return reinterpret_cast<const real *>(
         __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), src));
 }
-__device__ __forceinline__ float *shfl_ptr(float *p, int src) {
-    return reinterpret_cast<float *>(__shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), src));
+__device__ __forceinline__ real *shfl_ptr(real *p, int src) {
+    return reinterpret_cast<real *>(__shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), src));
 }
 
 // True when lane i's base is lane 0's base + i * STRIDE for all 32 lanes (a
@@ -58,18 +79,18 @@ __device__ __forceinline__ bool aligned16(const void *p) {
     return (reinterpret_cast<unsigned long long>(p) & 15ull) == 0;
 }
 
-// Coalesced gather of W floats per knot (knot-major) into stage[lane*W + j].
-// Contiguous tiles copy 32*W floats straight (float4 when aligned); other
+// Coalesced gather of W reals per knot (knot-major) into stage[lane*W + j].
+// Contiguous tiles copy 32*W reals straight (16-byte slots when aligned); other
 // tiles (idle lanes, trajectory boundaries) resolve every knot's base.
 template <int W>
-__device__ __forceinline__ void gather_in(float *stage, const float *base, int lane) {
-    const float *b0;
+__device__ __forceinline__ void gather_in(real *stage, const real *base, int lane) {
+    const real *b0;
     if (tile_contiguous<W>(base, lane, b0)) {
         if (aligned16(b0)) {
-            const float4 *src = reinterpret_cast<const float4 *>(b0);
-            float4 *dst = reinterpret_cast<float4 *>(stage);
+            const real4 *src = reinterpret_cast<const real4 *>(b0);
+            real4 *dst = reinterpret_cast<real4 *>(stage);
 #pragma unroll
-            for (int e = lane; e < 8 * W; e += 32) dst[e] = __ldg(src + e);
+            for (int e = lane; e < 8 * W; e += 32) dst[e] = ldg4(src + e);
         } else {
 #pragma unroll
             for (int e = lane; e < 32 * W; e += 32) stage[e] = __ldg(b0 + e);
@@ -79,22 +100,22 @@ __device__ __forceinline__ void gather_in(float *stage, const float *base, int l
 #pragma unroll
     for (int e = lane; e < 32 * W; e += 32) {
         const int kn = e / W, j = e - kn * W;
-        const float *p = shfl_ptr(base, kn);
+        const real *p = shfl_ptr(base, kn);
         stage[e] = p ? __ldg(p + j) : 0.0f;
     }
 }
 
-// Coalesced scatter of stage[lane*W + j] to each knot's W floats at base
-// (knots STRIDE floats apart).
+// Coalesced scatter of stage[lane*W + j] to each knot's W reals at base
+// (knots STRIDE reals apart).
 template <int W, int STRIDE = W>
-__device__ __forceinline__ void scatter_out(const float *stage, float *base, int lane) {
+__device__ __forceinline__ void scatter_out(const real *stage, real *base, int lane) {
     __syncwarp();
-    float *b0;
+    real *b0;
     if (tile_contiguous<STRIDE>(base, lane, b0)) {
         if constexpr (STRIDE == W) {
             if (aligned16(b0)) {
-                const float4 *src = reinterpret_cast<const float4 *>(stage);
-                float4 *dst = reinterpret_cast<float4 *>(b0);
+                const real4 *src = reinterpret_cast<const real4 *>(stage);
+                real4 *dst = reinterpret_cast<real4 *>(b0);
 #pragma unroll
                 for (int e = lane; e < 8 * W; e += 32) dst[e] = src[e];
             } else {
@@ -119,24 +140,24 @@ __device__ __forceinline__ void scatter_out(const float *stage, float *base, int
 #pragma unroll 7
         for (int e = lane; e < 32 * W; e += 32) {
             const int kn = e / W, j = e - kn * W;
-            float *p = shfl_ptr(base, kn);
+            real *p = shfl_ptr(base, kn);
             if (p) p[j] = stage[e];
         }
     }
     __syncwarp();
 }
 
-__device__ __forceinline__ void lds_link(const WarpSmem *ws, int k, int lane, float v[6], float Iv[6]) {
-    const float4 a = ws->link[kSlotsPerLink * k + 0][lane];
-    const float4 b = ws->link[kSlotsPerLink * k + 1][lane];
-    const float4 c = ws->link[kSlotsPerLink * k + 2][lane];
+__device__ __forceinline__ void lds_link(const WarpSmem *ws, int k, int lane, real v[6], real Iv[6]) {
+    const real4 a = ws->link[kSlotsPerLink * k + 0][lane];
+    const real4 b = ws->link[kSlotsPerLink * k + 1][lane];
+    const real4 c = ws->link[kSlotsPerLink * k + 2][lane];
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y;
     Iv[0] = b.z; Iv[1] = b.w; Iv[2] = c.x; Iv[3] = c.y; Iv[4] = c.z; Iv[5] = c.w;
 }
-__device__ __forceinline__ void sts_link(WarpSmem *ws, int k, int lane, const float v[6], const float Iv[6]) {
-    ws->link[kSlotsPerLink * k + 0][lane] = make_float4(v[0], v[1], v[2], v[3]);
-    ws->link[kSlotsPerLink * k + 1][lane] = make_float4(v[4], v[5], Iv[0], Iv[1]);
-    ws->link[kSlotsPerLink * k + 2][lane] = make_float4(Iv[2], Iv[3], Iv[4], Iv[5]);
+__device__ __forceinline__ void sts_link(WarpSmem *ws, int k, int lane, const real v[6], const real Iv[6]) {
+    ws->link[kSlotsPerLink * k + 0][lane] = make_real4(v[0], v[1], v[2], v[3]);
+    ws->link[kSlotsPerLink * k + 1][lane] = make_real4(v[4], v[5], Iv[0], Iv[1]);
+    ws->link[kSlotsPerLink * k + 2][lane] = make_real4(Iv[2], Iv[3], Iv[4], Iv[5]);
 }
 
 // sin and cos of a joint angle: the hardware approximation inside [-pi, pi]
@@ -146,43 +167,45 @@ __device__ __forceinline__ void sincos_angle(float x, float *s, float *c) {
     if (fabsf(x) <= 3.14159f) __sincosf(x, s, c);
     else sincosf(x, s, c);
 }
+// FP64 verification build: the double-precision library routine throughout.
+__device__ __forceinline__ void sincos_angle(double x, double *s, double *c) { sincos(x, s, c); }
 
 // ------------------------------------------------ articulated inertia ------
 
 // G = Rz N Rz^T for symmetric N (upper entries used), result symmetric.
-__device__ __forceinline__ void rotz_sym(float G[3][3], const float N[3][3], float c, float s) {
-    const float cc = c * c, ss = s * s, cs = c * s, d = cc - ss;
-    G[0][0] = fmaf(cc, N[0][0], fmaf(ss, N[1][1], -2.0f * cs * N[0][1]));
-    G[1][1] = fmaf(ss, N[0][0], fmaf(cc, N[1][1], 2.0f * cs * N[0][1]));
-    G[0][1] = fmaf(cs, N[0][0] - N[1][1], d * N[0][1]);
-    G[0][2] = fmaf(c, N[0][2], -s * N[1][2]);
-    G[1][2] = fmaf(s, N[0][2], c * N[1][2]);
+__device__ __forceinline__ void rotz_sym(real G[3][3], const real N[3][3], real c, real s) {
+    const real cc = c * c, ss = s * s, cs = c * s, d = cc - ss;
+    G[0][0] = fmaR(cc, N[0][0], fmaR(ss, N[1][1], -2.0f * cs * N[0][1]));
+    G[1][1] = fmaR(ss, N[0][0], fmaR(cc, N[1][1], 2.0f * cs * N[0][1]));
+    G[0][1] = fmaR(cs, N[0][0] - N[1][1], d * N[0][1]);
+    G[0][2] = fmaR(c, N[0][2], -s * N[1][2]);
+    G[1][2] = fmaR(s, N[0][2], c * N[1][2]);
     G[2][2] = N[2][2];
     G[1][0] = G[0][1]; G[2][0] = G[0][2]; G[2][1] = G[1][2];
 }
 
 // G = Rz N Rz^T for general N.
-__device__ __forceinline__ void rotz_gen(float G[3][3], const float N[3][3], float c, float s) {
-    float H[3][3];
+__device__ __forceinline__ void rotz_gen(real G[3][3], const real N[3][3], real c, real s) {
+    real H[3][3];
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-        H[0][j] = fmaf(c, N[0][j], -s * N[1][j]);
-        H[1][j] = fmaf(s, N[0][j], c * N[1][j]);
+        H[0][j] = fmaR(c, N[0][j], -s * N[1][j]);
+        H[1][j] = fmaR(s, N[0][j], c * N[1][j]);
         H[2][j] = N[2][j];
     }
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        G[i][0] = fmaf(c, H[i][0], -s * H[i][1]);
-        G[i][1] = fmaf(s, H[i][0], c * H[i][1]);
+        G[i][0] = fmaR(c, H[i][0], -s * H[i][1]);
+        G[i][1] = fmaR(s, H[i][0], c * H[i][1]);
         G[i][2] = H[i][2];
     }
 }
 
 // O = F^T G F:  O[i][j] = s_i s_j G[p_i][p_j]
-template <int k> __device__ __forceinline__ void perm_FT_G_F(float O[3][3], const float G[3][3]) {
+template <int k> __device__ __forceinline__ void perm_FT_G_F(real O[3][3], const real G[3][3]) {
     using J = Joint<k>;
     constexpr int p[3] = {J::p0, J::p1, J::p2};
-    constexpr float sg[3] = {J::s0, J::s1, J::s2};
+    constexpr real sg[3] = {J::s0, J::s1, J::s2};
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -193,56 +216,56 @@ template <int k> __device__ __forceinline__ void perm_FT_G_F(float O[3][3], cons
 // With At = E^T A E, Bt = E^T B E, Mt = E^T M E:
 //   M' = Mt,  B' = Bt + r^ Mt,  A' = At + r^ Bt^T - B' r^.
 template <int k>
-__device__ __forceinline__ void congruence(float Ao[3][3], float Bo[3][3], float Mo[3][3], const float A[3][3],
-                                           const float B[3][3], const float M[3][3], float c, float s) {
+__device__ __forceinline__ void congruence(real Ao[3][3], real Bo[3][3], real Mo[3][3], const real A[3][3],
+                                           const real B[3][3], const real M[3][3], real c, real s) {
     using J = Joint<k>;
-    float G[3][3], At[3][3], Bt[3][3];
+    real G[3][3], At[3][3], Bt[3][3];
     rotz_sym(G, A, c, s);
     perm_FT_G_F<k>(At, G);
     rotz_gen(G, B, c, s);
     perm_FT_G_F<k>(Bt, G);
     rotz_sym(G, M, c, s);
     perm_FT_G_F<k>(Mo, G);
-    const float t = J::t;
+    const real t = J::t;
     if constexpr (J::axis == 2) {
         // r^ = [0 -t 0; t 0 0; 0 0 0]
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            Bo[0][j] = fmaf(-t, Mo[1][j], Bt[0][j]);
-            Bo[1][j] = fmaf(t, Mo[0][j], Bt[1][j]);
+            Bo[0][j] = fmaR(-t, Mo[1][j], Bt[0][j]);
+            Bo[1][j] = fmaR(t, Mo[0][j], Bt[1][j]);
             Bo[2][j] = Bt[2][j];
         }
         // (r^ Bt^T)[i][j]: i=0: -t Bt[j][1]; i=1: t Bt[j][0]; i=2: 0
         // (B' r^)[i][j]:   j=0: t B'[i][1]; j=1: -t B'[i][0]; j=2: 0
-        Ao[0][0] = fmaf(-t, Bt[0][1], fmaf(-t, Bo[0][1], At[0][0]));
-        Ao[0][1] = fmaf(-t, Bt[1][1], fmaf(t, Bo[0][0], At[0][1]));
-        Ao[0][2] = fmaf(-t, Bt[2][1], At[0][2]);
-        Ao[1][1] = fmaf(t, Bt[1][0], fmaf(t, Bo[1][0], At[1][1]));
-        Ao[1][2] = fmaf(t, Bt[2][0], At[1][2]);
+        Ao[0][0] = fmaR(-t, Bt[0][1], fmaR(-t, Bo[0][1], At[0][0]));
+        Ao[0][1] = fmaR(-t, Bt[1][1], fmaR(t, Bo[0][0], At[0][1]));
+        Ao[0][2] = fmaR(-t, Bt[2][1], At[0][2]);
+        Ao[1][1] = fmaR(t, Bt[1][0], fmaR(t, Bo[1][0], At[1][1]));
+        Ao[1][2] = fmaR(t, Bt[2][0], At[1][2]);
         Ao[2][2] = At[2][2];
     } else {
         // r^ = [0 0 t; 0 0 0; -t 0 0]
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            Bo[0][j] = fmaf(t, Mo[2][j], Bt[0][j]);
+            Bo[0][j] = fmaR(t, Mo[2][j], Bt[0][j]);
             Bo[1][j] = Bt[1][j];
-            Bo[2][j] = fmaf(-t, Mo[0][j], Bt[2][j]);
+            Bo[2][j] = fmaR(-t, Mo[0][j], Bt[2][j]);
         }
         // (r^ Bt^T)[i][j]: i=0: t Bt[j][2]; i=1: 0; i=2: -t Bt[j][0]
         // (B' r^)[i][j]:   j=0: -t B'[i][2]; j=1: 0; j=2: t B'[i][0]
-        Ao[0][0] = fmaf(t, Bt[0][2], fmaf(t, Bo[0][2], At[0][0]));
-        Ao[0][1] = fmaf(t, Bt[1][2], At[0][1]);
-        Ao[0][2] = fmaf(t, Bt[2][2], fmaf(-t, Bo[0][0], At[0][2]));
+        Ao[0][0] = fmaR(t, Bt[0][2], fmaR(t, Bo[0][2], At[0][0]));
+        Ao[0][1] = fmaR(t, Bt[1][2], At[0][1]);
+        Ao[0][2] = fmaR(t, Bt[2][2], fmaR(-t, Bo[0][0], At[0][2]));
         Ao[1][1] = At[1][1];
-        Ao[1][2] = fmaf(-t, Bo[1][0], At[1][2]);
-        Ao[2][2] = fmaf(-t, Bt[2][0], fmaf(-t, Bo[2][0], At[2][2]));
+        Ao[1][2] = fmaR(-t, Bo[1][0], At[1][2]);
+        Ao[2][2] = fmaR(-t, Bt[2][0], fmaR(-t, Bo[2][0], At[2][2]));
     }
     Ao[1][0] = Ao[0][1]; Ao[2][0] = Ao[0][2]; Ao[2][1] = Ao[1][2];
 }
 
 // IA_k = I_k + child carry, as blocks [A B; B^T M].
 template <int k>
-__device__ __forceinline__ void add_link_inertia(float A[3][3], float B[3][3], float M[3][3]) {
+__device__ __forceinline__ void add_link_inertia(real A[3][3], real B[3][3], real M[3][3]) {
     using L = Link<k>;
     A[0][0] += L::Ixx; A[1][1] += L::Iyy; A[2][2] += L::Izz;
     A[0][1] += L::Ixy; A[1][0] += L::Ixy;
@@ -260,16 +283,16 @@ __device__ __forceinline__ void add_link_inertia(float A[3][3], float B[3][3], f
 // sincos, RNEA(q, qd, 0), bias, Minv (upper triangle, Mi[i][j] for i <= j), qdd.
 // Leaves v_k and I_k v_k of every link in the warp's link slots.
 template <bool DAMP, bool MPC, bool FEXT = false>
-__device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7], const float qd[7], const float u[7],
-                                       float sq[7], float cq[7], float Mi[7][7], float qdd[7],
-                                       const float *fx = nullptr) {
+__device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const real q[7], const real qd[7], const real u[7],
+                                       real sq[7], real cq[7], real Mi[7][7], real qdd[7],
+                                       const real *fx = nullptr) {
 #pragma unroll
     for (int k = 0; k < kJoints; k++) sincos_angle(q[k], &sq[k], &cq[k]);
 
     // RNEA forward with qdd = 0 (RNEA_fp, dynamicsGradient.h:620-659)
-    float f[kJoints][6];
+    real f[kJoints][6];
     {
-        float v[6], a[6];
+        real v[6], a[6];
         static_for<0, kJoints>([&](auto K) {
             constexpr int k = decltype(K)::value;
             if constexpr (k == 0) {
@@ -278,22 +301,22 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
 #pragma unroll
                     for (int i = 0; i < 6; i++) a[i] = 0.0f;
                 } else {
-                    const float g[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, kGravity};
+                    const real g[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, kGravity};
                     xmotion<0>(a, g, cq[0], sq[0]);
                 }
             } else {
-                float nv[6], na[6];
+                real nv[6], na[6];
                 xmotion<k>(nv, v, cq[k], sq[k]);
                 nv[2] += qd[k];
                 xmotion<k>(na, a, cq[k], sq[k]);
-                na[0] = fmaf(nv[1], qd[k], na[0]);
-                na[1] = fmaf(-nv[0], qd[k], na[1]);
-                na[3] = fmaf(nv[4], qd[k], na[3]);
-                na[4] = fmaf(-nv[3], qd[k], na[4]);
+                na[0] = fmaR(nv[1], qd[k], na[0]);
+                na[1] = fmaR(-nv[0], qd[k], na[1]);
+                na[3] = fmaR(nv[4], qd[k], na[3]);
+                na[4] = fmaR(-nv[3], qd[k], na[4]);
 #pragma unroll
                 for (int i = 0; i < 6; i++) { v[i] = nv[i]; a[i] = na[i]; }
             }
-            float Iv[6];
+            real Iv[6];
             imul<k>(Iv, v);
             imul<k>(f[k], a);
             crf_acc(f[k], v, Iv);
@@ -305,13 +328,13 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
         });
     }
     // backward (RNEA_bp :662-670) -> c, bias (computeBias :677-683)
-    float bias[kJoints];
+    real bias[kJoints];
     static_for_down<kJoints - 1, 0>([&](auto K) {
         constexpr int k = decltype(K)::value;
-        const float c = f[k][2];
-        bias[k] = DAMP ? u[k] - fmaf(0.5f, qd[k], c) : u[k] - c;
+        const real c = f[k][2];
+        bias[k] = DAMP ? u[k] - fmaR(0.5f, qd[k], c) : u[k] - c;
         if constexpr (k > 0) {
-            float t[6];
+            real t[6];
             xforce_T<k>(t, f[k], cq[k], sq[k]);
 #pragma unroll
             for (int i = 0; i < 6; i++) f[k - 1][i] += t[i];
@@ -320,9 +343,9 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
 
     // articulated-inertia sweep: U_k = IA_k[:,2], D_k = U_k[2]
     // (Minv_bp :424-436; compute_Ia_revolute :147; ctransform_Ia_revolute :222)
-    float U[kJoints][6], Dinv[kJoints];
+    real U[kJoints][6], Dinv[kJoints];
     {
-        float A[3][3], B[3][3], M[3][3];
+        real A[3][3], B[3][3], M[3][3];
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -335,17 +358,17 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
             Dinv[k] = 1.0f / U[k][2];
             if constexpr (k > 0) {
                 // Ia = IA - U U^T / D with the joint row/column exactly zero
-                float Ud[6];
+                real Ud[6];
 #pragma unroll
                 for (int i = 0; i < 6; i++) Ud[i] = U[k][i] * Dinv[k];
-                float Aa[3][3], Ba[3][3], Ma[3][3];
+                real Aa[3][3], Ba[3][3], Ma[3][3];
 #pragma unroll
                 for (int i = 0; i < 3; i++)
 #pragma unroll
                     for (int j = 0; j < 3; j++) {
-                        Aa[i][j] = (i == 2 || j == 2) ? 0.0f : fmaf(-U[k][i], Ud[j], A[i][j]);
-                        Ba[i][j] = (i == 2) ? 0.0f : fmaf(-U[k][i], Ud[3 + j], B[i][j]);
-                        Ma[i][j] = fmaf(-U[k][3 + i], Ud[3 + j], M[i][j]);
+                        Aa[i][j] = (i == 2 || j == 2) ? 0.0f : fmaR(-U[k][i], Ud[j], A[i][j]);
+                        Ba[i][j] = (i == 2) ? 0.0f : fmaR(-U[k][i], Ud[3 + j], B[i][j]);
+                        Ma[i][j] = fmaR(-U[k][3 + i], Ud[3 + j], M[i][j]);
                     }
                 congruence<k>(A, B, M, Aa, Ba, Ma, cq[k], sq[k]);
             }
@@ -356,7 +379,7 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
     // forward pass (fwdPassUpdate, :440-461), each column carrying one F vector.
     static_for<0, kJoints>([&](auto JJ) {
         constexpr int j = decltype(JJ)::value;
-        float F[6];
+        real F[6];
         static_for_down<j, 0>([&](auto II) {
             constexpr int i = decltype(II)::value;
             if constexpr (i == j) {
@@ -364,13 +387,13 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
 #pragma unroll
                 for (int r = 0; r < 6; r++) F[r] = U[j][r] * Dinv[j];
             } else {
-                const float m = -Dinv[i] * F[2];
+                const real m = -Dinv[i] * F[2];
                 Mi[i][j] = m;
 #pragma unroll
-                for (int r = 0; r < 6; r++) F[r] = fmaf(U[i][r], m, F[r]);
+                for (int r = 0; r < 6; r++) F[r] = fmaR(U[i][r], m, F[r]);
             }
             if constexpr (i > 0) {
-                float t[6];
+                real t[6];
                 xforce_T<i>(t, F, cq[i], sq[i]);
 #pragma unroll
                 for (int r = 0; r < 6; r++) F[r] = t[r];
@@ -384,12 +407,12 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
                 F[2] = Mi[0][j];
             } else {
                 // Minv[i][j] -= D_i^-1 U_i^T X_i F_{i-1};  F_i = S Minv[i][j] + X_i F_{i-1}
-                float y[6];
+                real y[6];
                 xmotion<i>(y, F, cq[i], sq[i]);
-                float d = U[i][0] * y[0];
+                real d = U[i][0] * y[0];
 #pragma unroll
-                for (int r = 1; r < 6; r++) d = fmaf(U[i][r], y[r], d);
-                Mi[i][j] = fmaf(-Dinv[i], d, Mi[i][j]);
+                for (int r = 1; r < 6; r++) d = fmaR(U[i][r], y[r], d);
+                Mi[i][j] = fmaR(-Dinv[i], d, Mi[i][j]);
 #pragma unroll
                 for (int r = 0; r < 6; r++) F[r] = y[r];
                 F[2] += Mi[i][j];
@@ -400,9 +423,9 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
     // qdd = Minv_sym bias (matVMultSym, math.h:29-37)
 #pragma unroll
     for (int r = 0; r < kJoints; r++) {
-        float acc = 0.0f;
+        real acc = 0.0f;
 #pragma unroll
-        for (int k = 0; k < kJoints; k++) acc = fmaf(r <= k ? Mi[r][k] : Mi[k][r], bias[k], acc);
+        for (int k = 0; k < kJoints; k++) acc = fmaR(r <= k ? Mi[r][k] : Mi[k][r], bias[k], acc);
         qdd[r] = acc;
     }
 }
@@ -411,32 +434,32 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const float q[7],
 // accumulated f_k[0,1,3,4] in the link slots (read at the diagonal step of the
 // d/dq sweeps).
 template <bool MPC, bool FEXT = false>
-__device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const float qd[7], const float qdd[7],
-                                              const float sq[7], const float cq[7], const float *fx = nullptr) {
-    float f[kJoints][6];
-    float a[6];
+__device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const real qd[7], const real qdd[7],
+                                              const real sq[7], const real cq[7], const real *fx = nullptr) {
+    real f[kJoints][6];
+    real a[6];
     static_for<0, kJoints>([&](auto K) {
         constexpr int k = decltype(K)::value;
-        float v[6], Iv[6];
+        real v[6], Iv[6];
         lds_link(ws, k, lane, v, Iv);
         if constexpr (k == 0) {
             if constexpr (MPC) {
 #pragma unroll
                 for (int i = 0; i < 6; i++) a[i] = 0.0f;
             } else {
-                const float g[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, kGravity};
+                const real g[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, kGravity};
                 xmotion<0>(a, g, cq[0], sq[0]);
             }
             a[2] += qdd[0];
         } else {
-            float xa[6];
+            real xa[6];
             xmotion<k>(xa, a, cq[k], sq[k]);
-            ws->link[kSlotsPerLink * k + 3][lane] = make_float4(xa[0], xa[1], xa[3], xa[4]);
-            a[0] = fmaf(v[1], qd[k], xa[0]);
-            a[1] = fmaf(-v[0], qd[k], xa[1]);
+            ws->link[kSlotsPerLink * k + 3][lane] = make_real4(xa[0], xa[1], xa[3], xa[4]);
+            a[0] = fmaR(v[1], qd[k], xa[0]);
+            a[1] = fmaR(-v[0], qd[k], xa[1]);
             a[2] = xa[2] + qdd[k];
-            a[3] = fmaf(v[4], qd[k], xa[3]);
-            a[4] = fmaf(-v[3], qd[k], xa[4]);
+            a[3] = fmaR(v[4], qd[k], xa[3]);
+            a[4] = fmaR(-v[3], qd[k], xa[4]);
             a[5] = xa[5];
         }
         imul<k>(f[k], a);
@@ -448,8 +471,8 @@ __device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const floa
     });
     static_for_down<kJoints - 1, 1>([&](auto K) {
         constexpr int k = decltype(K)::value;
-        ws->link[kSlotsPerLink * k + 4][lane] = make_float4(f[k][0], f[k][1], f[k][3], f[k][4]);
-        float t[6];
+        ws->link[kSlotsPerLink * k + 4][lane] = make_real4(f[k][0], f[k][1], f[k][3], f[k][4]);
+        real t[6];
         xforce_T<k>(t, f[k], cq[k], sq[k]);
 #pragma unroll
         for (int i = 0; i < 6; i++) f[k - 1][i] += t[i];
@@ -463,9 +486,9 @@ __device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const floa
 // df_k = I_k da + dv x* (I_k v_k) + v_k x* (I_k dv): the force tangent of
 // link k from its velocity / acceleration tangents (dv, da).
 template <int k>
-__device__ __forceinline__ void link_force_tangent(float df[6], const float v[6], const float Iv[6],
-                                                   const float dv[6], const float da[6]) {
-    float Idv[6];
+__device__ __forceinline__ void link_force_tangent(real df[6], const real v[6], const real Iv[6],
+                                                   const real dv[6], const real da[6]) {
+    real Idv[6];
     imul<k>(Idv, dv);
     imul<k>(df, da);
     crf_acc(df, dv, Iv);
@@ -479,26 +502,26 @@ __device__ __forceinline__ void link_force_tangent(float df[6], const float v[6]
 // tangents of link k, two independent dependency chains in one basic block
 // (the link loop is unrolled, the column c is a warp-uniform runtime value).
 template <bool QSIDE, bool DAMP>
-__device__ __forceinline__ void dtau_column(const WarpSmem *ws, int lane, int c, const float qd[7],
-                                            const float sq[7], const float cq[7], float dtau[7]) {
-    float df[kJoints][6];
-    float dv[6], da[6];
+__device__ __forceinline__ void dtau_column(const WarpSmem *ws, int lane, int c, const real qd[7],
+                                            const real sq[7], const real cq[7], real dtau[7]) {
+    real df[kJoints][6];
+    real dv[6], da[6];
     static_for<0, kJoints>([&](auto K) {
         constexpr int k = decltype(K)::value;
         if (k == c) {
-            float v[6], Iv[6];
+            real v[6], Iv[6];
             lds_link(ws, k, lane, v, Iv);
             if constexpr (QSIDE) {
                 // dv = crm(X_k v_{k-1}) S; (X_k v_{k-1}) and v_k agree outside entry 2
                 dv[0] = v[1]; dv[1] = -v[0]; dv[2] = 0.0f;
                 dv[3] = v[4]; dv[4] = -v[3]; dv[5] = 0.0f;
                 // da = crm(dv) S qd_k + crm(X_k a_{k-1}) S
-                const float4 xa = ws->link[kSlotsPerLink * k + 3][lane];  // (Xa0, Xa1, Xa3, Xa4)
-                da[0] = fmaf(dv[1], qd[k], xa.y);
-                da[1] = fmaf(-dv[0], qd[k], -xa.x);
+                const real4 xa = ws->link[kSlotsPerLink * k + 3][lane];  // (Xa0, Xa1, Xa3, Xa4)
+                da[0] = fmaR(dv[1], qd[k], xa.y);
+                da[1] = fmaR(-dv[0], qd[k], -xa.x);
                 da[2] = 0.0f;
-                da[3] = fmaf(dv[4], qd[k], xa.w);
-                da[4] = fmaf(-dv[3], qd[k], -xa.z);
+                da[3] = fmaR(dv[4], qd[k], xa.w);
+                da[4] = fmaR(-dv[3], qd[k], -xa.z);
                 da[5] = 0.0f;
             } else {
                 // dv = S, da = crm(v_k) S
@@ -508,27 +531,27 @@ __device__ __forceinline__ void dtau_column(const WarpSmem *ws, int lane, int c,
             }
         } else if (k > c) {
             if constexpr (k >= 1) {
-                float v[6], Iv[6];
+                real v[6], Iv[6];
                 lds_link(ws, k - 1, lane, v, Iv);
                 link_force_tangent<k - 1>(df[k - 1], v, Iv, dv, da);
-                float ndv[6], nda[6];
+                real ndv[6], nda[6];
                 xmotion<k>(ndv, dv, cq[k], sq[k]);
                 xmotion<k>(nda, da, cq[k], sq[k]);
-                nda[0] = fmaf(ndv[1], qd[k], nda[0]);
-                nda[1] = fmaf(-ndv[0], qd[k], nda[1]);
-                nda[3] = fmaf(ndv[4], qd[k], nda[3]);
-                nda[4] = fmaf(-ndv[3], qd[k], nda[4]);
+                nda[0] = fmaR(ndv[1], qd[k], nda[0]);
+                nda[1] = fmaR(-ndv[0], qd[k], nda[1]);
+                nda[3] = fmaR(ndv[4], qd[k], nda[3]);
+                nda[4] = fmaR(-ndv[3], qd[k], nda[4]);
 #pragma unroll
                 for (int i = 0; i < 6; i++) { dv[i] = ndv[i]; da[i] = nda[i]; }
             }
         }
     });
     {
-        float v[6], Iv[6];
+        real v[6], Iv[6];
         lds_link(ws, kJoints - 1, lane, v, Iv);
         link_force_tangent<kJoints - 1>(df[kJoints - 1], v, Iv, dv, da);
     }
-    float dF[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    real dF[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     static_for_down<kJoints - 1, 0>([&](auto K) {
         constexpr int k = decltype(K)::value;
         if (k >= c) {
@@ -539,10 +562,10 @@ __device__ __forceinline__ void dtau_column(const WarpSmem *ws, int lane, int c,
         if constexpr (k > 0) {
             if (QSIDE && k == c) {
                 // + X_k^T (S x* f_k)
-                const float4 fs = ws->link[kSlotsPerLink * k + 4][lane];  // (f0, f1, f3, f4)
+                const real4 fs = ws->link[kSlotsPerLink * k + 4][lane];  // (f0, f1, f3, f4)
                 dF[0] -= fs.y; dF[1] += fs.x; dF[3] -= fs.w; dF[4] += fs.z;
             }
-            float t[6];
+            real t[6];
             xforce_T<k>(t, dF, cq[k], sq[k]);
 #pragma unroll
             for (int i = 0; i < 6; i++) dF[i] = t[i];
@@ -552,12 +575,12 @@ __device__ __forceinline__ void dtau_column(const WarpSmem *ws, int lane, int c,
 }
 
 // out = -Minv_sym dtau
-__device__ __forceinline__ void minv_times(float out[7], const float Mi[7][7], const float dtau[7]) {
+__device__ __forceinline__ void minv_times(real out[7], const real Mi[7][7], const real dtau[7]) {
 #pragma unroll
     for (int r = 0; r < kJoints; r++) {
-        float acc = 0.0f;
+        real acc = 0.0f;
 #pragma unroll
-        for (int k = 0; k < kJoints; k++) acc = fmaf(r <= k ? Mi[r][k] : Mi[k][r], dtau[k], acc);
+        for (int k = 0; k < kJoints; k++) acc = fmaR(r <= k ? Mi[r][k] : Mi[k][r], dtau[k], acc);
         out[r] = -acc;
     }
 }
@@ -570,7 +593,7 @@ __device__ __forceinline__ void minv_times(float out[7], const float Mi[7][7], c
 template <bool DAMP, bool MPC, bool MIRROR = false, bool FEXT = false, bool FDONLY = false>
 __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotPtrs &kp,
                                              const KnotPtrs &mr = KnotPtrs{}) {
-    float q[7], qd[7], u[7];
+    real q[7], qd[7], u[7];
     gather_in<7>(ws->stage, kp.q, lane);
     gather_in<7>(ws->stage + 224, kp.qd, lane);
     gather_in<7>(ws->stage + 448, kp.u, lane);
@@ -583,18 +606,18 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     }
     __syncwarp();
     if constexpr (MIRROR) {
-        scatter_out<7>(ws->stage, const_cast<float *>(mr.q), lane);
-        scatter_out<7>(ws->stage + 224, const_cast<float *>(mr.qd), lane);
-        scatter_out<7>(ws->stage + 448, const_cast<float *>(mr.u), lane);
+        scatter_out<7>(ws->stage, const_cast<real *>(mr.q), lane);
+        scatter_out<7>(ws->stage + 224, const_cast<real *>(mr.qd), lane);
+        scatter_out<7>(ws->stage + 448, const_cast<real *>(mr.u), lane);
     }
-    const float *fx = nullptr;
-    if constexpr (FEXT) {  // the lane's 42 external-force floats stay staged through both RNEA passes
+    const real *fx = nullptr;
+    if constexpr (FEXT) {  // the lane's 42 external-force values stay staged through both RNEA passes
         gather_in<42>(ws->stage, kp.fext, lane);
         __syncwarp();
         fx = ws->stage + lane * 42;
     }
 
-    float sq[7], cq[7], Mi[7][7], qdd[7];
+    real sq[7], cq[7], Mi[7][7], qdd[7];
     phase1<DAMP, MPC, FEXT>(ws, lane, q, qd, u, sq, cq, Mi, qdd, fx);
     // with FEXT the second RNEA runs while the forces are still staged;
     // otherwise after the Minv / qdd stores (fewer live registers)
@@ -624,7 +647,7 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r] = 0.0f;
 #pragma unroll 1
     for (int c = 1; c < kJoints; c++) {
-        float dtau[7], out[7];
+        real dtau[7], out[7];
         dtau_column<true, DAMP>(ws, lane, c, qd, sq, cq, dtau);
         minv_times(out, Mi, dtau);
 #pragma unroll
@@ -635,7 +658,7 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     // d qdd / dqd: columns 7..13
 #pragma unroll 1
     for (int c = 0; c < kJoints; c++) {
-        float dtau[7], out[7];
+        real dtau[7], out[7];
         dtau_column<false, DAMP>(ws, lane, c, qd, sq, cq, dtau);
         minv_times(out, Mi, dtau);
 #pragma unroll
@@ -645,4 +668,4 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd ? mr.dqdd + 49 : nullptr, lane);
 }
 
-}  // namespace frg
+}  // namespace FRG_NS

@@ -15,10 +15,26 @@
 #pragma once
 #include <cuda_runtime.h>
 
-namespace frg {
+// Scalar type of the device code: float for the engine; the FP64 verification
+// build (frg_f64_kernels.cu) compiles the same code with FRG_REAL=double into
+// namespace frg64.
+#ifndef FRG_REAL
+#define FRG_REAL float
+#endif
+#ifndef FRG_NS
+#define FRG_NS frg
+#endif
+
+namespace FRG_NS {
+
+using real = FRG_REAL;
+__device__ __forceinline__ real fmaR(real a, real b, real c) {
+    if constexpr (sizeof(real) == sizeof(float)) return fmaf(a, b, c);
+    else return fma(a, b, c);
+}
 
 constexpr int kJoints = 7;
-constexpr float kGravity = 9.81f;  // GRAVITY default, dynamicsGradient.h:7-9
+constexpr real kGravity = real(9.81);  // GRAVITY default, dynamicsGradient.h:7-9
 
 template <int N> struct IC { static constexpr int value = N; };
 
@@ -58,14 +74,14 @@ constexpr LinkInertial kLinks[kJoints] = {
 // dynamicsGradient.h:78-118), coupling m c, mass m.
 template <int k> struct Link {
     static constexpr LinkInertial L = kLinks[k];
-    static constexpr float Ixx = float(L.ixx + L.m * (L.cy * L.cy + L.cz * L.cz));
-    static constexpr float Iyy = float(L.iyy + L.m * (L.cx * L.cx + L.cz * L.cz));
-    static constexpr float Izz = float(L.izz + L.m * (L.cx * L.cx + L.cy * L.cy));
-    static constexpr float Ixy = float(L.ixy - L.m * L.cx * L.cy);
-    static constexpr float Ixz = float(L.ixz - L.m * L.cx * L.cz);
-    static constexpr float Iyz = float(L.iyz - L.m * L.cy * L.cz);
-    static constexpr float mcx = float(L.m * L.cx), mcy = float(L.m * L.cy), mcz = float(L.m * L.cz);
-    static constexpr float m = float(L.m);
+    static constexpr real Ixx = real(L.ixx + L.m * (L.cy * L.cy + L.cz * L.cz));
+    static constexpr real Iyy = real(L.iyy + L.m * (L.cx * L.cx + L.cz * L.cz));
+    static constexpr real Izz = real(L.izz + L.m * (L.cx * L.cx + L.cy * L.cy));
+    static constexpr real Ixy = real(L.ixy - L.m * L.cx * L.cy);
+    static constexpr real Ixz = real(L.ixz - L.m * L.cx * L.cz);
+    static constexpr real Iyz = real(L.iyz - L.m * L.cy * L.cz);
+    static constexpr real mcx = real(L.m * L.cx), mcy = real(L.m * L.cy), mcz = real(L.m * L.cz);
+    static constexpr real m = real(L.m);
 };
 
 // Joint frames (utils/iiwa_14.urdf iiwa_joint_1..7 <origin>).  F maps w to
@@ -75,34 +91,34 @@ template <int k> struct Link {
 //   rpy (pi/2,0,0):              p = {0,2,1}, s = {+,-,+}   w -> (w0, w2, -w1)
 // Translations as tz_j1..ty_j7, dynamicsGradient.h:223-229.
 template <int k> struct Joint;
-template <> struct Joint<0> { static constexpr int p0 = 0, p1 = 1, p2 = 2; static constexpr float s0 = 1, s1 = 1, s2 = 1; static constexpr int axis = 2; static constexpr float t = 0.1575f; };
-template <> struct Joint<1> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 2; static constexpr float t = 0.2025f; };
-template <> struct Joint<2> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr float t = 0.2045f; };
-template <> struct Joint<3> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = 1, s1 = -1, s2 = 1; static constexpr int axis = 2; static constexpr float t = 0.2155f; };
-template <> struct Joint<4> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr float t = 0.1845f; };
-template <> struct Joint<5> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = 1, s1 = -1, s2 = 1; static constexpr int axis = 2; static constexpr float t = 0.2155f; };
-template <> struct Joint<6> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr float s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr float t = 0.081f; };
+template <> struct Joint<0> { static constexpr int p0 = 0, p1 = 1, p2 = 2; static constexpr real s0 = 1, s1 = 1, s2 = 1; static constexpr int axis = 2; static constexpr real t = real(0.1575); };
+template <> struct Joint<1> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 2; static constexpr real t = real(0.2025); };
+template <> struct Joint<2> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr real t = real(0.2045); };
+template <> struct Joint<3> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = 1, s1 = -1, s2 = 1; static constexpr int axis = 2; static constexpr real t = real(0.2155); };
+template <> struct Joint<4> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr real t = real(0.1845); };
+template <> struct Joint<5> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = 1, s1 = -1, s2 = 1; static constexpr int axis = 2; static constexpr real t = real(0.2155); };
+template <> struct Joint<6> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr real t = real(0.081); };
 
 // ------------------------------------------------------- 3-vector pieces ---
 
 // E w = Rz(q)^T (F w)
-template <int k> __device__ __forceinline__ void rot_E(float o[3], const float w[3], float c, float s) {
+template <int k> __device__ __forceinline__ void rot_E(real o[3], const real w[3], real c, real s) {
     using J = Joint<k>;
-    float fw[3];
+    real fw[3];
     fw[J::p0] = J::s0 * w[0];
     fw[J::p1] = J::s1 * w[1];
     fw[J::p2] = J::s2 * w[2];
-    o[0] = fmaf(c, fw[0], s * fw[1]);
-    o[1] = fmaf(c, fw[1], -s * fw[0]);
+    o[0] = fmaR(c, fw[0], s * fw[1]);
+    o[1] = fmaR(c, fw[1], -s * fw[0]);
     o[2] = fw[2];
 }
 
 // E^T w = F^T (Rz(q) w),  (F^T x)_i = s_i x[p_i]
-template <int k> __device__ __forceinline__ void rot_ET(float o[3], const float w[3], float c, float s) {
+template <int k> __device__ __forceinline__ void rot_ET(real o[3], const real w[3], real c, real s) {
     using J = Joint<k>;
-    float x[3];
-    x[0] = fmaf(c, w[0], -s * w[1]);
-    x[1] = fmaf(c, w[1], s * w[0]);
+    real x[3];
+    x[0] = fmaR(c, w[0], -s * w[1]);
+    x[1] = fmaR(c, w[1], s * w[0]);
     x[2] = w[2];
     o[0] = J::s0 * x[J::p0];
     o[1] = J::s1 * x[J::p1];
@@ -110,61 +126,61 @@ template <int k> __device__ __forceinline__ void rot_ET(float o[3], const float 
 }
 
 // o = u - r x w  (r = t e_axis)
-template <int k> __device__ __forceinline__ void sub_r_cross(float o[3], const float u[3], const float w[3]) {
+template <int k> __device__ __forceinline__ void sub_r_cross(real o[3], const real u[3], const real w[3]) {
     using J = Joint<k>;
     if constexpr (J::axis == 2) {  // r x w = (-t w1, t w0, 0)
-        o[0] = fmaf(J::t, w[1], u[0]);
-        o[1] = fmaf(-J::t, w[0], u[1]);
+        o[0] = fmaR(J::t, w[1], u[0]);
+        o[1] = fmaR(-J::t, w[0], u[1]);
         o[2] = u[2];
     } else {  // axis y: r x w = (t w2, 0, -t w0)
-        o[0] = fmaf(-J::t, w[2], u[0]);
+        o[0] = fmaR(-J::t, w[2], u[0]);
         o[1] = u[1];
-        o[2] = fmaf(J::t, w[0], u[2]);
+        o[2] = fmaR(J::t, w[0], u[2]);
     }
 }
 
 // o = u + r x w
-template <int k> __device__ __forceinline__ void add_r_cross(float o[3], const float u[3], const float w[3]) {
+template <int k> __device__ __forceinline__ void add_r_cross(real o[3], const real u[3], const real w[3]) {
     using J = Joint<k>;
     if constexpr (J::axis == 2) {
-        o[0] = fmaf(-J::t, w[1], u[0]);
-        o[1] = fmaf(J::t, w[0], u[1]);
+        o[0] = fmaR(-J::t, w[1], u[0]);
+        o[1] = fmaR(J::t, w[0], u[1]);
         o[2] = u[2];
     } else {
-        o[0] = fmaf(J::t, w[2], u[0]);
+        o[0] = fmaR(J::t, w[2], u[0]);
         o[1] = u[1];
-        o[2] = fmaf(-J::t, w[0], u[2]);
+        o[2] = fmaR(-J::t, w[0], u[2]);
     }
 }
 
 // ------------------------------------------------------- spatial vectors ---
 
 // y = X_k x  (motion vector to the child frame):  [E w; E (v - r x w)]
-template <int k> __device__ __forceinline__ void xmotion(float y[6], const float x[6], float c, float s) {
-    float u[3];
+template <int k> __device__ __forceinline__ void xmotion(real y[6], const real x[6], real c, real s) {
+    real u[3];
     rot_E<k>(y, x, c, s);
     sub_r_cross<k>(u, x + 3, x);
     rot_E<k>(y + 3, u, c, s);
 }
 
 // y = X_k^T x  (force vector to the parent frame):  [E^T n + r x (E^T f); E^T f]
-template <int k> __device__ __forceinline__ void xforce_T(float y[6], const float x[6], float c, float s) {
-    float n[3];
+template <int k> __device__ __forceinline__ void xforce_T(real y[6], const real x[6], real c, real s) {
+    real n[3];
     rot_ET<k>(y + 3, x + 3, c, s);
     rot_ET<k>(n, x, c, s);
     add_r_cross<k>(y, n, y + 3);
 }
 
 #define FRG_ACC(acc, K, x)                   \
-    if constexpr ((K) != 0.0f) {             \
-        acc = fmaf((K), (x), acc);           \
+    if constexpr ((K) != real(0)) {             \
+        acc = fmaR((K), (x), acc);           \
     }
 
 // y = I_k w:  [Ibar w + mc x v; m v - mc x w]
-template <int k> __device__ __forceinline__ void imul(float y[6], const float x[6]) {
+template <int k> __device__ __forceinline__ void imul(real y[6], const real x[6]) {
     using L = Link<k>;
-    const float w0 = x[0], w1 = x[1], w2 = x[2], v0 = x[3], v1 = x[4], v2 = x[5];
-    float t0 = L::Ixx * w0, t1 = L::Iyy * w1, t2 = L::Izz * w2;
+    const real w0 = x[0], w1 = x[1], w2 = x[2], v0 = x[3], v1 = x[4], v2 = x[5];
+    real t0 = L::Ixx * w0, t1 = L::Iyy * w1, t2 = L::Izz * w2;
     FRG_ACC(t0, L::Ixy, w1) FRG_ACC(t0, L::Ixz, w2)
     FRG_ACC(t1, L::Ixy, w0) FRG_ACC(t1, L::Iyz, w2)
     FRG_ACC(t2, L::Ixz, w0) FRG_ACC(t2, L::Iyz, w1)
@@ -172,7 +188,7 @@ template <int k> __device__ __forceinline__ void imul(float y[6], const float x[
     FRG_ACC(t0, L::mcy, v2) FRG_ACC(t0, -L::mcz, v1)
     FRG_ACC(t1, L::mcz, v0) FRG_ACC(t1, -L::mcx, v2)
     FRG_ACC(t2, L::mcx, v1) FRG_ACC(t2, -L::mcy, v0)
-    float b0 = L::m * v0, b1 = L::m * v1, b2 = L::m * v2;
+    real b0 = L::m * v0, b1 = L::m * v1, b2 = L::m * v2;
     // - mc x w
     FRG_ACC(b0, -L::mcy, w2) FRG_ACC(b0, L::mcz, w1)
     FRG_ACC(b1, -L::mcz, w0) FRG_ACC(b1, L::mcx, w2)
@@ -181,20 +197,20 @@ template <int k> __device__ __forceinline__ void imul(float y[6], const float x[
 }
 
 // y = I_k S = I_k e_2 (third column, constant)
-template <int k> __device__ __forceinline__ void icol2(float y[6]) {
+template <int k> __device__ __forceinline__ void icol2(real y[6]) {
     using L = Link<k>;
     y[0] = L::Ixz; y[1] = L::Iyz; y[2] = L::Izz;
     y[3] = -L::mcy; y[4] = L::mcx; y[5] = 0.0f;
 }
 
 // y += crf(v) h = v x* h
-__device__ __forceinline__ void crf_acc(float y[6], const float v[6], const float h[6]) {
-    y[0] = fmaf(v[1], h[2], fmaf(-v[2], h[1], fmaf(v[4], h[5], fmaf(-v[5], h[4], y[0]))));
-    y[1] = fmaf(v[2], h[0], fmaf(-v[0], h[2], fmaf(v[5], h[3], fmaf(-v[3], h[5], y[1]))));
-    y[2] = fmaf(v[0], h[1], fmaf(-v[1], h[0], fmaf(v[3], h[4], fmaf(-v[4], h[3], y[2]))));
-    y[3] = fmaf(v[1], h[5], fmaf(-v[2], h[4], y[3]));
-    y[4] = fmaf(v[2], h[3], fmaf(-v[0], h[5], y[4]));
-    y[5] = fmaf(v[0], h[4], fmaf(-v[1], h[3], y[5]));
+__device__ __forceinline__ void crf_acc(real y[6], const real v[6], const real h[6]) {
+    y[0] = fmaR(v[1], h[2], fmaR(-v[2], h[1], fmaR(v[4], h[5], fmaR(-v[5], h[4], y[0]))));
+    y[1] = fmaR(v[2], h[0], fmaR(-v[0], h[2], fmaR(v[5], h[3], fmaR(-v[3], h[5], y[1]))));
+    y[2] = fmaR(v[0], h[1], fmaR(-v[1], h[0], fmaR(v[3], h[4], fmaR(-v[4], h[3], y[2]))));
+    y[3] = fmaR(v[1], h[5], fmaR(-v[2], h[4], y[3]));
+    y[4] = fmaR(v[2], h[3], fmaR(-v[0], h[5], y[4]));
+    y[5] = fmaR(v[0], h[4], fmaR(-v[1], h[3], y[5]));
 }
 
-}  // namespace frg
+}  // namespace FRG_NS

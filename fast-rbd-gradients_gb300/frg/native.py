@@ -34,7 +34,7 @@ EXPORTED = (
     "frg_host_alloc", "frg_host_free", "frg_gradient_ragged_noalloc", "frg_server_options_default",
     "frg_server_create", "frg_server_destroy", "frg_server_submit", "frg_server_poll", "frg_server_wait",
     "frg_server_wait_any", "frg_server_release", "frg_server_get_stats", "frg_gradient_fext",
-    "frg_forward_dynamics", "frg_discrete_jacobians",
+    "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64",
 )
 
 
@@ -121,6 +121,8 @@ def _declare(L):
         "frg_gradient_fext": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
         "frg_forward_dynamics": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp]),
         "frg_discrete_jacobians": (st, [vp, i32, vp, vp, ctypes.c_float, vp, vp, vp]),
+        "frg_gradient_f64": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp]),
+        "frg_verify_f64": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -280,6 +282,17 @@ class Context:
         """Explicit-Euler A [n][14x14], B [n][14x7] from dqdd and minv (device buffers)."""
         self._check(lib().frg_discrete_jacobians(self._h, int(n_knots), _ptr(dqdd), _ptr(minv), float(dt), _ptr(A),
                                                  _ptr(B), _stream_ptr(stream)), "frg_discrete_jacobians")
+
+    def gradient_f64(self, n_knots, q, qd, u, dqdd, qdd, minv, stream=None):
+        """FP64 verification build of the plain path (device double buffers)."""
+        self._check(lib().frg_gradient_f64(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd),
+                                           _ptr(minv), _stream_ptr(stream)), "frg_gradient_f64")
+
+    def verify_f64(self, n_knots, q, qd, u, dqdd, qdd, minv, err, stream=None):
+        """Per-knot Frobenius-relative errors err [n,3] (device doubles) of the
+        FP32 results dqdd, qdd, minv against the FP64 build on the same inputs."""
+        self._check(lib().frg_verify_f64(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd),
+                                         _ptr(minv), _ptr(err), _stream_ptr(stream)), "frg_verify_f64")
 
     def gradient_host_into(self, n_knots, q, qd, u, dqdd, qdd, minv):
         """Host-buffer path: inputs in, outputs written to the given host arrays."""

@@ -8,7 +8,8 @@ bench_latency():   closed-loop saturation, then Poisson arrivals at 50 % of
 bench_admission(): 20,000 sessions queued at once, horizons U{8..512}, 10
                    calls each, device pool capped at 2 GiB so admission
                    throttles; throughput, p50/p99, admission stalls, and 1 %
-                   of calls checked against the FP64 CPU oracle.
+                   of calls verified by the FP64 GPU build (frg_verify_f64),
+                   cross-checked against the FP64 CPU oracle when one is given.
 """
 import ctypes
 import os
@@ -120,14 +121,40 @@ def bench_admission(ctx, sessions=20000, pool_bytes=2 << 30, oracle=None):
                     "p99_us", "max_us", "mean_batch_requests"))
     out.update(admission_stalls=stats["admission_stalls"], pool_bytes_cap=stats["pool_bytes_cap"],
                pool_bytes_peak=stats["pool_bytes_peak"], launches=stats["launches"])
-    if oracle is not None and "sample" in r and len(r["sample"]["q"]):
+    if "sample" in r and len(r["sample"]["q"]):
         s = r["sample"]
-        rd, rq, rm = oracle.gradient_f64(s["q"], s["qd"], s["u"])
-        out["fp64_check"] = {
+        err, ms = verify_f64_gpu(ctx, s)
+        chk = {
             "sampled_calls": int(len(s["h"])), "sampled_knots": int(len(s["q"])),
-            "max_frob_rel_dqdd": float(oracle.frob_rel(s["dqdd"], rd).max()),
-            "max_frob_rel_qdd": float(oracle.frob_rel(s["qdd"], rq).max()),
-            "max_frob_rel_minv": float(oracle.frob_rel(s["minv"], rm).max()),
-            "where": "CPU FP64 oracle on 1 % of calls (no FP64 GPU kernel)",
+            "max_frob_rel_dqdd": float(err[:, 0].max()),
+            "max_frob_rel_qdd": float(err[:, 1].max()),
+            "max_frob_rel_minv": float(err[:, 2].max()),
+            "gpu_verify_ms": round(ms, 3),
+            "where": "FP64 GPU verification build (frg_verify_f64) on 1 % of calls, after the run",
         }
+        if oracle is not None:
+            # the same per-knot errors against the FP64 CPU oracle
+            ref = oracle.gradient_f64(s["q"], s["qd"], s["u"])
+            host = np.stack([oracle.frob_rel(s[k], x) for k, x in zip(("dqdd", "qdd", "minv"), ref)], axis=1)
+            chk["cpu_oracle_max_abs_diff"] = float(np.abs(host - err).max())
+        out["fp64_check"] = chk
     return out
+
+
+def verify_f64_gpu(ctx, s):
+    """Per-knot FP64 errors [n, 3] of sampled FP32 results, on the GPU; and the
+    device time of one verification call (ms), its scratch already sized."""
+    import torch
+    n = len(s["q"])
+    t = {k: torch.from_numpy(np.ascontiguousarray(s[k], np.float32)).cuda()
+         for k in ("q", "qd", "u", "dqdd", "qdd", "minv")}
+    err = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    args = (n, t["q"], t["qd"], t["u"], t["dqdd"], t["qdd"], t["minv"], err)
+    ctx.verify_f64(*args, stream=st)  # sizes the context's FP64 scratch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    ctx.verify_f64(*args, stream=st)
+    e1.record(st)
+    st.synchronize()
+    return err.cpu().numpy(), e0.elapsed_time(e1)

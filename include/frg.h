@@ -134,6 +134,27 @@ frg_status frg_forward_dynamics(frg_ctx *ctx, int n_knots, const float *q, const
 frg_status frg_discrete_jacobians(frg_ctx *ctx, int n_knots, const float *dqdd, const float *minv, float dt,
                                   float *A, float *B, frg_stream stream);
 
+/*
+ * FP64 verification build (DEVICE arrays, asynchronous on `stream`).  The
+ * reference's GPU path is FP32 only and has no counterpart; its FP64 results
+ * come from the CPU recursions (helpers_CPU/dynamicsGradient.h:916-934 with
+ * T = double), which these calls restate on the device from the same kernel
+ * source compiled in double.
+ *  - frg_gradient_f64: frg_gradient with double arrays of the same layouts.
+ *  - frg_verify_f64: recomputes n_knots knots in FP64 from the FP32 inputs q,
+ *    qd, u and writes, per knot, the Frobenius-relative errors
+ *    ||x - x64||_F / ||x64||_F of the FP32 results dqdd, qdd, minv to
+ *    err [n][3] (doubles, device).  Its scratch (175 doubles per knot) is a
+ *    ctx-owned device buffer that grows on demand: a call that grows it
+ *    allocates and synchronises the device, so size it once with the largest
+ *    batch before timed or captured work.  Calls sharing a ctx must not
+ *    overlap on different streams.
+ */
+frg_status frg_gradient_f64(frg_ctx *ctx, int n_knots, const double *q, const double *qd, const double *u,
+                            double *dqdd, double *qdd, double *minv, frg_stream stream);
+frg_status frg_verify_f64(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                          const float *dqdd, const float *qdd, const float *minv, double *err, frg_stream stream);
+
 /* One trajectory (a contiguous run of knots) of a batched call; all DEVICE
  * pointers with the layouts above. */
 typedef struct frg_traj {
