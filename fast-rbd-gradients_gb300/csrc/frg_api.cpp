@@ -428,7 +428,6 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
         const size_t need = n * (98 + 7 + 49);
         if (need > ctx->host_buf_floats) {
             cudaFree(ctx->host_buf);
-        cudaFree(ctx->f64_buf);
             ctx->host_buf = nullptr;
             ctx->host_buf_floats = 0;
             if (cudaMalloc(&ctx->host_buf, need * sizeof(float)) != cudaSuccess) {
@@ -471,7 +470,6 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
     const size_t need = n * (3 * 7 + 98 + 7 + 49);
     if (need > ctx->host_buf_floats) {
         cudaFree(ctx->host_buf);
-        cudaFree(ctx->f64_buf);
         ctx->host_buf = nullptr;
         ctx->host_buf_floats = 0;
         if (cudaMalloc(&ctx->host_buf, need * sizeof(float)) != cudaSuccess) {

@@ -116,3 +116,22 @@ def test_f64_argument_errors():
         with pytest.raises(frg.FrgError) as ei:
             ctx.verify_f64(-1, x, x, x, x, x, x, x)
         assert ei.value.status == 1
+
+
+def test_verify_f64_scratch_survives_host_calls():
+    """The FP64 scratch and the host-call staging are separate context buffers:
+    growing one leaves the other valid (verify, host call, verify smaller and
+    larger)."""
+    import torch
+    with frg.Context() as ctx:
+        for n in (500, 3000, 200, 5000):
+            q, qd, u = frg.sample_knots(n, seed=n)
+            tq, tqd, tu = (torch.from_numpy(a).cuda() for a in (q, qd, u))
+            out = [torch.empty((n, w), device="cuda") for w in (98, 7, 49)]
+            err = torch.empty((n, 3), device="cuda", dtype=torch.float64)
+            ctx.gradient(n, tq, tqd, tu, *out)
+            ctx.verify_f64(n, tq, tqd, tu, *out, err)
+            torch.cuda.synchronize()
+            assert float(err.max()) <= TOL
+            hd, hq, hm = ctx.gradient_host(q, qd, u)  # grows the staging buffer
+            assert np.array_equal(hq, out[1].cpu().numpy())
