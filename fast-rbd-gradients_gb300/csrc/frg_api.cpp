@@ -209,8 +209,6 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
         !check(ctx, frg::init_ext_kernels(), "fext / forward-dynamics kernel set-up") ||
         !check(ctx, frg::init_f64_kernels(), "FP64 kernel set-up") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
-        !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream2, cudaStreamNonBlocking), "cudaStreamCreate") ||
-        !check(ctx, cudaEventCreateWithFlags(&ctx->io_fork, cudaEventDisableTiming), "cudaEventCreate") ||
         !check(ctx, cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming), "cudaEventCreate")) {
         g_orphan_error = ctx->err;
         frg_destroy(ctx);
@@ -236,11 +234,6 @@ void frg_destroy(frg_ctx *ctx) {
         cudaFree(ctx->host_buf);
         cudaFree(ctx->f64_buf);
         if (ctx->io_stream) cudaStreamDestroy(ctx->io_stream);
-        if (ctx->io_stream2) {
-            cudaStreamSynchronize(ctx->io_stream2);
-            cudaStreamDestroy(ctx->io_stream2);
-        }
-        if (ctx->io_fork) cudaEventDestroy(ctx->io_fork);
         if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
     }
     delete ctx;
@@ -418,14 +411,15 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
     DeviceGuard g(ctx->device);
     cudaStream_t s = ctx->io_stream;
     const size_t n = static_cast<size_t>(n_knots);
-    // Pinned host arrays: the kernel reads q, qd, u across the host link
-    // itself, and the results leave in chunks -- chunk i's kernel writes to
-    // device staging, then its device-to-host copies run on the copy engine
-    // while chunk i + 1 computes on the other stream.  The host link (about
-    // 200 GB/s each way here) bounds this call, and the kernel hides behind it.
+    // Pinned host arrays: one launch and no copies.  The kernel reads q, qd,
+    // u across the host link and writes qdd and Minv in place as whole
+    // 16-byte-aligned tiles; dqdd goes through a device buffer (L2-resident
+    // while its tile finishes) and leaves as whole lines (launch_host_out).
+    // The results stream out while later tiles compute, so the host link's
+    // device-to-host rate (about 190 GB/s here) bounds the call.
     if (device_accessible(q) && device_accessible(qd) && device_accessible(u) && device_accessible(dqdd) &&
         device_accessible(qdd) && device_accessible(minv)) {
-        const size_t need = n * (98 + 7 + 49);
+        const size_t need = 98 * n;
         if (need > ctx->host_buf_floats) {
             cudaFree(ctx->host_buf);
             ctx->host_buf = nullptr;
@@ -437,32 +431,11 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
             }
             ctx->host_buf_floats = need;
         }
-        float *odqdd = ctx->host_buf, *oqdd = odqdd + 98 * n, *ominv = oqdd + 7 * n;
-        // 3 chunks of whole tiles (at least 4096 knots each): measured best
-        // between per-copy overheads and the exposed first / last chunk
-        size_t chunk = std::max<size_t>(4096, (n / 3 + 31) / 32 * 32);
-        cudaStream_t st[2] = {ctx->io_stream, ctx->io_stream2};
-        if (!check(ctx, cudaEventRecord(ctx->io_fork, st[0]), "event record") ||
-            !check(ctx, cudaStreamWaitEvent(st[1], ctx->io_fork, 0), "stream wait"))
-            return FRG_ERR_CUDA;
-        int i = 0;
-        for (size_t k0 = 0; k0 < n; k0 += chunk, i++) {
-            const size_t m = std::min(chunk, n - k0);
-            cudaStream_t sc = st[i & 1];
-            if (!check(ctx,
-                       frg::launch_plain(ctx->damping, ctx->mpc, ctx->shape, static_cast<int>(m), q + 7 * k0,
-                                         qd + 7 * k0, u + 7 * k0, odqdd + 98 * k0, oqdd + 7 * k0, ominv + 49 * k0, sc),
-                       "frg_gradient_host launch") ||
-                !check(ctx, cudaMemcpyAsync(dqdd + 98 * k0, odqdd + 98 * k0, 98 * m * sizeof(float),
-                                            cudaMemcpyDeviceToHost, sc), "D2H dqdd") ||
-                !check(ctx, cudaMemcpyAsync(qdd + 7 * k0, oqdd + 7 * k0, 7 * m * sizeof(float), cudaMemcpyDeviceToHost, sc),
-                       "D2H qdd") ||
-                !check(ctx, cudaMemcpyAsync(minv + 49 * k0, ominv + 49 * k0, 49 * m * sizeof(float),
-                                            cudaMemcpyDeviceToHost, sc), "D2H minv"))
-                return FRG_ERR_CUDA;
-        }
-        if (!check(ctx, cudaStreamSynchronize(st[1]), "frg_gradient_host sync") ||
-            !check(ctx, cudaStreamSynchronize(st[0]), "frg_gradient_host sync"))
+        if (!check(ctx,
+                   frg::launch_host_out(ctx->damping, ctx->mpc, ctx->shape, n_knots, q, qd, u, ctx->host_buf, dqdd,
+                                        qdd, minv, s),
+                   "frg_gradient_host launch") ||
+            !check(ctx, cudaStreamSynchronize(s), "frg_gradient_host sync"))
             return FRG_ERR_CUDA;
         return FRG_OK;
     }

@@ -52,9 +52,7 @@ struct frg_ctx {
     int num_sms = 0;
     std::string err;
     cudaStream_t io_stream = nullptr;   // frg_gradient_host
-    cudaStream_t io_stream2 = nullptr;  // second stream of its chunk pipeline
-    cudaEvent_t io_fork = nullptr;
-    float *host_buf = nullptr;          // device staging for frg_gradient_host
+    float *host_buf = nullptr;          // device staging for frg_gradient_host (dqdd relay / pageable path)
     size_t host_buf_floats = 0;
     DeviceBatch scratch;                // frg_gradient_batched descriptors
     double *f64_buf = nullptr;          // frg_verify_f64 scratch (175 doubles per knot)

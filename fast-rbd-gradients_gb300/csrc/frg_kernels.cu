@@ -17,6 +17,7 @@ struct PlainArgs {
     const float *q, *qd, *u;
     float *dqdd, *qdd, *minv;
     int n;
+    float *dqdd_relay = nullptr;  // RELAY: final dqdd destination (host memory)
 };
 
 __device__ __forceinline__ KnotPtrs plain_knot(const PlainArgs &a, int tile, int lane) {
@@ -25,7 +26,38 @@ __device__ __forceinline__ KnotPtrs plain_knot(const PlainArgs &a, int tile, int
     return KnotPtrs{a.q + 7 * g, a.qd + 7 * g, a.u + 7 * g, a.dqdd + 98 * g, a.qdd + 7 * g, a.minv + 49 * g};
 }
 
-template <bool DAMP, bool MPC>
+// Floats of `p` that precede it in its 128-byte line.  A warp loop over
+// e = lane - line_shift(p) + 32 m stores exactly one whole line per step,
+// which keeps stores to memory that is off 16-byte alignment at full rate
+// over the host link (partial lines cost about 30 % there).
+__device__ __forceinline__ int line_shift(const float *p) {
+    return static_cast<int>((reinterpret_cast<unsigned long long>(p) & 127ull) / sizeof(float));
+}
+
+// Copies a finished tile's dqdd rows (98 floats per knot, contiguous) from
+// the device array to their final place.  Over the host link only whole
+// aligned lines write at full rate: the two 49-float halves at a 98-float
+// stride that process_tile stores run at about 60 % of it, so host results go
+// through device memory (where the tile is still in L2) and leave as one
+// contiguous 12.5 KB run of 16-byte stores.
+__device__ __forceinline__ void relay_dqdd(const PlainArgs &a, int tile, int lane) {
+    const long long k0 = static_cast<long long>(tile) * 32;
+    const int m = a.n - k0 < 32 ? static_cast<int>(a.n - k0) : 32;
+    const float *src = a.dqdd + 98 * k0;  // written by this warp: plain loads, not the read-only path
+    float *dst = a.dqdd_relay + 98 * k0;
+    if (m == 32 && aligned16(src) && aligned16(dst)) {
+        const float4 *s4 = reinterpret_cast<const float4 *>(src);
+        float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll 5
+        for (int e = lane; e < 98 * 32 / 4; e += 32) d4[e] = s4[e];
+    } else {
+        for (int e = lane - line_shift(dst); e < 98 * m; e += 32)
+            if (e >= 0) dst[e] = src[e];
+    }
+    __syncwarp();
+}
+
+template <bool DAMP, bool MPC, bool RELAY = false>
 __global__ void __launch_bounds__(kMaxWarpsPerCta * 32) grad_plain_kernel(PlainArgs a) {
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -35,6 +67,8 @@ __global__ void __launch_bounds__(kMaxWarpsPerCta * 32) grad_plain_kernel(PlainA
     for (int tile = blockIdx.x * warps_per_cta + warp; tile < ntiles; tile += gridDim.x * warps_per_cta) {
         const KnotPtrs kp = plain_knot(a, tile, lane);
         process_tile<DAMP, MPC>(ws, lane, kp);
+        // scatter_out ended with __syncwarp: every lane's dqdd stores are visible to the warp
+        if constexpr (RELAY) relay_dqdd(a, tile, lane);
     }
 }
 
@@ -83,12 +117,12 @@ cudaError_t prepare(K kernel) {
                                 cudaSharedmemCarveoutMaxShared);
 }
 
-template <bool D, bool M>
+template <bool D, bool M, bool R = false>
 cudaError_t plain_impl(const LaunchShape &sh, const PlainArgs &a, cudaStream_t st) {
     const int warps = sh.warps_per_cta;
     const int ntiles = (a.n + 31) / 32;
     const int grid = (ntiles + warps - 1) / warps;
-    grad_plain_kernel<D, M><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(a);
+    grad_plain_kernel<D, M, R><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -113,6 +147,8 @@ cudaError_t init_kernels() {
     cudaError_t e = cudaSuccess;
     for (cudaError_t r : {prepare(grad_plain_kernel<false, false>), prepare(grad_plain_kernel<true, false>),
                           prepare(grad_plain_kernel<false, true>), prepare(grad_plain_kernel<true, true>),
+                          prepare(grad_plain_kernel<false, false, true>), prepare(grad_plain_kernel<true, false, true>),
+                          prepare(grad_plain_kernel<false, true, true>), prepare(grad_plain_kernel<true, true, true>),
                           prepare(grad_ragged_kernel<false, false>), prepare(grad_ragged_kernel<true, false>),
                           prepare(grad_ragged_kernel<false, true>), prepare(grad_ragged_kernel<true, true>)})
         if (r != cudaSuccess && e == cudaSuccess) e = r;
@@ -141,6 +177,21 @@ cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n
     if (damping && !mpc) return plain_impl<true, false>(shape, a, stream);
     if (!damping && mpc) return plain_impl<false, true>(shape, a, stream);
     return plain_impl<true, true>(shape, a, stream);
+}
+
+cudaError_t launch_host_out(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
+                            const float *u, float *dqdd_dev, float *dqdd, float *qdd, float *minv,
+                            cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    if (shape.warps_per_cta < 1 || shape.warps_per_cta > kMaxWarpsPerCta) return cudaErrorInvalidValue;
+    if (shape.lanes_per_knot == 8)  // small batches: latency first, every result straight to its destination
+        return launch_group_plain(damping, mpc, shape, n, q, qd, u, dqdd, qdd, minv, stream);
+    PlainArgs a{q, qd, u, dqdd_dev, qdd, minv, n};
+    a.dqdd_relay = dqdd;
+    if (!damping && !mpc) return plain_impl<false, false, true>(shape, a, stream);
+    if (damping && !mpc) return plain_impl<true, false, true>(shape, a, stream);
+    if (!damping && mpc) return plain_impl<false, true, true>(shape, a, stream);
+    return plain_impl<true, true, true>(shape, a, stream);
 }
 
 cudaError_t launch_ragged(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const Segment *segs,

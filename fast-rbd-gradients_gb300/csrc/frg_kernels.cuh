@@ -44,6 +44,14 @@ int max_ctas_per_sm(int warps, int lanes_per_knot = 1);
 cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
                          const float *u, float *dqdd, float *qdd, float *minv, cudaStream_t stream);
 
+// Plain path for results in host memory (pinned, mapped): q, qd, u, qdd and
+// minv are read and written in place across the host link; dqdd is computed
+// into dqdd_dev (device, [n][98]) and each finished tile is copied to dqdd as
+// whole lines.  The latency mapping writes every result in place directly.
+cudaError_t launch_host_out(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
+                            const float *u, float *dqdd_dev, float *dqdd, float *qdd, float *minv,
+                            cudaStream_t stream);
+
 // Ragged batch: one persistent launch walking 32-knot tiles of the
 // concatenated knot list.  segs[nseg + 1] (last = end sentinel with
 // knot_begin = total knots), tile_seg[ntiles] = segment of each tile's first

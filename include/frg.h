@@ -106,10 +106,11 @@ frg_status frg_gradient(frg_ctx *ctx, int n_knots, const float *q, const float *
 /*
  * Same, for HOST arrays, synchronous: returns when the results are in the host
  * arrays (the time_GPU.cu:313-316 "Compute + I/O" sequence).  Pinned arrays
- * (frg_host_alloc, cudaHostAlloc / cudaHostRegister) take a pipelined path:
- * the kernel reads the inputs across the host link itself and the results are
- * copied back in chunks that overlap the next chunk's arithmetic; pageable
- * arrays are staged through device buffers owned by ctx.
+ * (frg_host_alloc, cudaHostAlloc / cudaHostRegister) take a single launch
+ * with no copies: the kernel reads the inputs across the host link itself and
+ * writes each 32-knot tile's results to the host arrays as soon as the tile
+ * finishes, so the transfer overlaps the arithmetic.  Pageable arrays are
+ * staged through device buffers owned by ctx.
  */
 frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
                              float *dqdd, float *qdd, float *minv);

@@ -140,25 +140,34 @@ def test_latency_mapping_parity(golden, damping, mpc, n):
     assert max_err(g[0], golden[f"dqdd_{tag}"]) <= TOL and max_err(g[2], golden[f"minv_{tag}"]) <= TOL
 
 
-def test_host_call_pinned_zero_copy_equals_staged():
-    """frg_gradient_host on pinned buffers (kernel reads/writes host memory
-    directly) gives the same bits as on pageable buffers (staged copies)."""
+@pytest.mark.parametrize("n,lanes,offset", [(1, 1, 0), (31, 1, 0), (3000, 1, 0), (70001, 1, 0), (3000, 1, 1),
+                                             (3000, 8, 0), (45, 8, 1)])
+def test_host_call_pinned_zero_copy_equals_staged(n, lanes, offset):
+    """frg_gradient_host on pinned buffers (the kernel reads inputs from host
+    memory and writes results there, dqdd relayed through device memory as
+    whole tiles) gives the same bits as on pageable buffers (staged copies):
+    whole and partial tiles, both thread mappings, and host arrays that start
+    one float off 16-byte alignment (the relay's element-wise branch)."""
     import ctypes
-    n = 3000
-    q, qd, u = frg.sample_knots(n, seed=31)
+    q, qd, u = frg.sample_knots(n, seed=31 + n)
     L = frg.lib()
     bufs = {}
     for name, w in (("q", 7), ("qd", 7), ("u", 7), ("dqdd", 98), ("qdd", 7), ("minv", 49)):
-        ptr = L.frg_host_alloc(4 * w * n)
+        ptr = L.frg_host_alloc(4 * (w * n + offset))
         assert ptr
-        bufs[name] = (ptr, np.ctypeslib.as_array((ctypes.c_float * (w * n)).from_address(ptr)).reshape(n, w))
+        addr = ptr + 4 * offset
+        arr = np.ctypeslib.as_array((ctypes.c_float * (w * n)).from_address(addr)).reshape(n, w)
+        bufs[name] = (ptr, addr, arr)
     try:
-        bufs["q"][1][:], bufs["qd"][1][:], bufs["u"][1][:] = q, qd, u
+        bufs["q"][2][:], bufs["qd"][2][:], bufs["u"][2][:] = q, qd, u
+        for k in ("dqdd", "qdd", "minv"):
+            bufs[k][2][:] = np.nan
         with frg.Context() as ctx:
+            ctx.set_lanes_per_knot(lanes)
             staged = ctx.gradient_host(q, qd, u)
-            ctx.gradient_host_into(n, *(bufs[k][0] for k in ("q", "qd", "u", "dqdd", "qdd", "minv")))
+            ctx.gradient_host_into(n, *(bufs[k][1] for k in ("q", "qd", "u", "dqdd", "qdd", "minv")))
         for name, ref in zip(("dqdd", "qdd", "minv"), staged):
-            assert np.array_equal(bufs[name][1], ref)
+            assert np.array_equal(bufs[name][2], ref), name
     finally:
-        for ptr, _ in bufs.values():
+        for ptr, _, _ in bufs.values():
             L.frg_host_free(ptr)
