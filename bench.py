@@ -13,7 +13,9 @@ through the full path (RNEA, Minv, q̈, dtau/dq, dtau/dqd, -Minv dtau) in FP32.
             D2H of dqdd, qdd, Minv inside every timed step.
   plain     the plain form of the same mix: one launch per trajectory.
   plain_scaling  one plain launch per batch of N contiguous knots, N in
-            {16, 32, 64, 128, 1024, 65536}, the faster thread mapping kept.
+            {16, 32, 64, 128, 1024, 65536} (L2 warm), plus N = 1 (single-knot
+            latency) and N = 65536 over batches larger than L2; the faster
+            thread mapping kept.
   served    p50/p99 request latency of the continuous-batching server, and
             the 2 GiB-pool admission run with 1 % of its calls verified by
             the FP64 GPU build.
@@ -162,27 +164,34 @@ class ClockSampler:
 
 
 PLAIN_SIZES = (16, 32, 64, 128, 1024, 65536)
+FLUSH_SETS = 4  # rotating 65,536-knot sets: 4 x 46 MB > 129 MB L2
 
 
 def plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak, steps=20):
     """Plain path, one launch per batch of N contiguous device-resident knots
-    (BASELINE's scaling config), in both thread mappings; the faster is kept."""
+    (the scaling config), in both thread mappings; the faster is kept.  Rows:
+    N = 1 (single-knot latency), every N of the config with one batch reused
+    (L2 warm), and N = 65,536 again over rotating batches larger than L2."""
     import frg
     out = []
-    q, qd, u = frg.sample_knots(max(PLAIN_SIZES), seed=99)
-    tq, tqd, tu = (torch.from_numpy(x).to(dev) for x in (q, qd, u))
-    o = [torch.empty((max(PLAIN_SIZES), w), device=dev) for w in (98, 7, 49)]
-    saved = ctx.lanes_per_knot()
-    for n in PLAIN_SIZES:
+    nmax = max(PLAIN_SIZES)
+    sets = []
+    for i in range(FLUSH_SETS):
+        q, qd, u = frg.sample_knots(nmax, seed=99 + i)
+        sets.append([torch.from_numpy(x).to(dev) for x in (q, qd, u)] +
+                    [torch.empty((nmax, w), device=dev) for w in (98, 7, 49)])
+    saved = ctx.tuning()
+    rows = [(1, 1)] + [(n, 1) for n in PLAIN_SIZES] + [(nmax, FLUSH_SETS)]
+    for n, nsets in rows:
         best = None
         for lanes in (1, 8):
             ctx.set_lanes_per_knot(lanes)
-            for _ in range(3):
-                ctx.gradient(n, tq, tqd, tu, *o, stream=stream)
+            for i in range(3):
+                ctx.gradient(n, *sets[i % nsets], stream=stream)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            for _ in range(steps):
-                ctx.gradient(n, tq, tqd, tu, *o, stream=stream)
+            for i in range(steps):
+                ctx.gradient(n, *sets[i % nsets], stream=stream)
             e1.record(stream)
             stream.synchronize()
             ms = e0.elapsed_time(e1) / steps
@@ -191,9 +200,11 @@ def plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak, steps=20):
         ms, lanes = best
         out.append({"n": n, "us_per_launch": round(ms * 1e3, 2), "knots_per_s": n / (ms * 1e-3),
                     "lanes_per_knot": lanes,
+                    "l2": "warm (one batch reused)" if nsets == 1 else
+                          f"flushed ({nsets} rotating batches, {nsets * n * BYTES_PER_KNOT / 1e6:.0f} MB)",
                     "hbm_frac": BYTES_PER_KNOT * n / (ms * 1e-3) / 1e9 / float(peaks["hbm_gbs"]),
                     "fp32_frac": FLOP_PER_KNOT_REF * n / (ms * 1e-3) / 1e12 / fp32_peak})
-    ctx.set_lanes_per_knot(saved)
+    ctx.set_tuning(saved)
     return out
 
 
@@ -214,17 +225,28 @@ def mix_parity(ctx, torch, sets, n, stream):
 
 def cpu_baseline(q, qd, u, budget_s=8.0):
     """The oracle port (C restatement of the reference CPU path) on all host
-    threads, on a bounded sample of the workload's knots."""
+    threads, on a bounded sample of the workload's knots: the full path
+    (q̈, Minv and the gradient timed: the figure comparable with the GPU), and
+    the reference's own time_CPU mode (q̈ and Minv passed in, untimed)."""
     import frg_oracle
     threads = os.cpu_count() or 1
     m = min(len(q), 16384)
     qs, qds, us = q[:m], qd[:m], u[:m]
-    t, _ = frg_oracle.time_threaded_f32(qs, qds, us, threads, 1)  # warm
-    iters = max(1, int(budget_s / max(t, 1e-3)))
-    t, _ = frg_oracle.time_threaded_f32(qs, qds, us, threads, iters)
+    out = None
+    for given in (False, True):
+        fn = frg_oracle.time_threaded_given_f32 if given else frg_oracle.time_threaded_f32
+        t, _ = fn(qs, qds, us, threads, 1)  # warm
+        iters = max(1, int(budget_s / 2 / max(t, 1e-3)))
+        t, _ = fn(qs, qds, us, threads, iters)
+        sample = f"{m} knots of the mix x {iters} rounds ({t:.1f} s), FP32, damping off, gravity on"
+        if not given:
+            out = {"value": m * iters / t, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                   "mode": "full path: q̈, Minv and the gradient timed"}
+        else:
+            out["time_cpu_mode"] = {"value": m * iters / t, "unit": UNIT, "sample": sample,
+                                    "mode": "the reference's time_CPU mode: q̈ and Minv passed in, not timed"}
     frg_oracle.shutdown_pool()
-    return {"value": m * iters / t, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{m} knots of the mix x {iters} rounds ({t:.1f} s), FP32, damping off, gravity on"}
+    return out
 
 
 def run_reference(args):
@@ -282,6 +304,7 @@ def run_frg(args):
         return 0
     tuned = None if args.profile else ctx.autotune(n)
     shape = ctx.launch_shape()
+    tuning = ctx.tuning()  # plain and persistent shapes chosen by frg_autotune
 
     # Trajectories live in memory in a shuffled order (as separately produced
     # trajectories do), so the batch is a ragged list of scattered runs that
@@ -408,8 +431,7 @@ def run_frg(args):
                             f"ragged trajectory list, replayed as a CUDA graph",
                 "knots_per_step": n, "l2": f"{ROTATING_SETS} rotating input/output sets "
                                             f"({ROTATING_SETS * n * BYTES_PER_KNOT / 1e6:.0f} MB > 129 MB L2)",
-                "launch_shape": {"plain": {"warps_per_cta": shape[0], "lanes_per_knot": ctx.lanes_per_knot()},
-                                 "persistent": "autotuned separately (frg_autotune)"},
+                "launch_shape": tuning,
                 "autotune_knots_per_s": tuned, "parallelism": f"replicas x{ws} (knots sharded, no collective)",
             },
             "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 84 * n, "d2h_bytes_per_step": 616 * n,

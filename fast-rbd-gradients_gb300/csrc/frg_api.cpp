@@ -333,6 +333,22 @@ frg_status frg_discrete_jacobians(frg_ctx *ctx, int n_knots, const float *dqdd, 
     return FRG_OK;
 }
 
+frg_status frg_knot_status(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                           const float *dqdd, const float *qdd, const float *minv, uint32_t *status,
+                           frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 0 || (n_knots > 0 && !(q && qd && u && status))) {
+        frg_set_error(ctx, "frg_knot_status: negative n_knots or null input / status pointer");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n_knots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    if (!check(ctx, frg::launch_knot_status(ctx->num_sms, n_knots, q, qd, u, dqdd, qdd, minv, status, stream),
+               "frg_knot_status launch"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
 frg_status frg_gradient_f64(frg_ctx *ctx, int n_knots, const double *q, const double *qd, const double *u,
                             double *dqdd, double *qdd, double *minv, frg_stream stream) {
     if (!ctx) return FRG_ERR_INVALID_ARGUMENT;

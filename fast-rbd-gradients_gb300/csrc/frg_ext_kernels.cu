@@ -52,6 +52,27 @@ __global__ void discretize_kernel(int n, const float *dqdd, const float *minv, f
     }
 }
 
+// status[k] |= bit for every non-finite element of a knot-major array of W
+// floats per knot (element-parallel and coalesced; atomics only on hits).
+template <int W>
+__device__ __forceinline__ void flag_nonfinite(const float *a, long long n, unsigned int bit, unsigned int *status) {
+    if (!a) return;
+    const long long total = n * W;
+    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<long long>(gridDim.x) * blockDim.x)
+        if (!isfinite(a[e])) atomicOr(status + e / W, bit);
+}
+
+__global__ void knot_status_kernel(long long n, const float *q, const float *qd, const float *u, const float *dqdd,
+                                   const float *qdd, const float *minv, unsigned int *status) {
+    flag_nonfinite<7>(q, n, 1u, status);
+    flag_nonfinite<7>(qd, n, 1u, status);
+    flag_nonfinite<7>(u, n, 1u, status);
+    flag_nonfinite<98>(dqdd, n, 2u, status);
+    flag_nonfinite<7>(qdd, n, 2u, status);
+    flag_nonfinite<49>(minv, n, 2u, status);
+}
+
 template <typename K>
 cudaError_t opt_in(K kernel) {
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -112,6 +133,18 @@ cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     discretize_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(n, dqdd, minv, dt, A, B);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_knot_status(int num_sms, int n, const float *q, const float *qd, const float *u,
+                               const float *dqdd, const float *qdd, const float *minv, unsigned int *status,
+                               cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned int) * static_cast<size_t>(n), stream);
+    if (e != cudaSuccess) return e;
+    long long blocks = (static_cast<long long>(n) * 98 + 255) / 256;
+    if (blocks > static_cast<long long>(num_sms) * 8) blocks = static_cast<long long>(num_sms) * 8;
+    knot_status_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(n, q, qd, u, dqdd, qdd, minv, status);
     return cudaGetLastError();
 }
 

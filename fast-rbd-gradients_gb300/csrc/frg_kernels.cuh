@@ -87,6 +87,10 @@ cudaError_t launch_ext(bool damping, bool mpc, const LaunchShape &shape, int n, 
                        cudaStream_t stream);
 cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float dt, float *A, float *B,
                               cudaStream_t stream);
+// Per-knot non-finite flags (bit 0 inputs, bit 1 outputs; NULL arrays skipped).
+cudaError_t launch_knot_status(int num_sms, int n, const float *q, const float *qd, const float *u,
+                               const float *dqdd, const float *qdd, const float *minv, unsigned int *status,
+                               cudaStream_t stream);
 
 // FP64 verification build (frg_f64_kernels.cu): the plain path in double, and
 // the two helpers of the sampled check of FP32 results (float inputs widened to

@@ -224,4 +224,39 @@ frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s)
     return FRG_OK;
 }
 
+frg_status frg_get_tuning(const frg_ctx *ctx, frg_tuning *out) {
+    if (!ctx || !out) return FRG_ERR_INVALID_ARGUMENT;
+    out->warps_per_cta = ctx->shape.warps_per_cta;
+    out->lanes_per_knot = ctx->shape.lanes_per_knot;
+    out->ragged_warps_per_cta = ctx->ragged_shape.warps_per_cta;
+    out->ragged_ctas_per_sm = ctx->ragged_shape.ctas_per_sm;
+    out->ragged_lanes_per_knot = ctx->ragged_shape.lanes_per_knot;
+    return FRG_OK;
+}
+
+frg_status frg_set_tuning(frg_ctx *ctx, const frg_tuning *t) {
+    if (!ctx || !t) return FRG_ERR_INVALID_ARGUMENT;
+    const int wmax = frg::max_warps_per_cta();
+    auto lanes_ok = [](int l) { return l == 1 || l == 8; };
+    bool good = t->warps_per_cta >= 1 && t->warps_per_cta <= wmax && lanes_ok(t->lanes_per_knot) &&
+                t->ragged_warps_per_cta >= 1 && t->ragged_warps_per_cta <= wmax &&
+                lanes_ok(t->ragged_lanes_per_knot) && t->ragged_ctas_per_sm >= 1;
+    if (good) {
+        DeviceGuard g(ctx->device);
+        const int occ = frg::max_ctas_per_sm(t->ragged_warps_per_cta, t->ragged_lanes_per_knot);
+        good = occ <= 0 || t->ragged_ctas_per_sm <= occ;
+    }
+    if (!good) {
+        frg_set_error(ctx, "frg_set_tuning: warps per CTA in [1, 8], lanes per knot 1 or 8, resident CTAs per SM "
+                           "in [1, occupancy]");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    ctx->shape.warps_per_cta = t->warps_per_cta;
+    ctx->shape.lanes_per_knot = t->lanes_per_knot;
+    ctx->ragged_shape.warps_per_cta = t->ragged_warps_per_cta;
+    ctx->ragged_shape.ctas_per_sm = t->ragged_ctas_per_sm;
+    ctx->ragged_shape.lanes_per_knot = t->ragged_lanes_per_knot;
+    return FRG_OK;
+}
+
 }  // extern "C"

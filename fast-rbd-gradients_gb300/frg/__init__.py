@@ -8,6 +8,8 @@ library is missing.
 from .inputs import JOINT_LIMITS, NUM_JOINTS, perturb, ragged_horizons, sample_knots  # noqa: F401
 from .native import (  # noqa: F401
     DQDD_FLOATS,
+    KNOT_NONFINITE_INPUT,
+    KNOT_NONFINITE_OUTPUT,
     MINV_FLOATS,
     Context,
     FrgError,

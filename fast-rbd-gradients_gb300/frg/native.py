@@ -34,8 +34,12 @@ EXPORTED = (
     "frg_host_alloc", "frg_host_free", "frg_gradient_ragged_noalloc", "frg_server_options_default",
     "frg_server_create", "frg_server_destroy", "frg_server_submit", "frg_server_poll", "frg_server_wait",
     "frg_server_wait_any", "frg_server_release", "frg_server_get_stats", "frg_gradient_fext",
-    "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64",
+    "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64", "frg_get_tuning",
+    "frg_set_tuning", "frg_knot_status",
 )
+
+KNOT_NONFINITE_INPUT = 1
+KNOT_NONFINITE_OUTPUT = 2
 
 
 class FrgError(RuntimeError):
@@ -53,6 +57,12 @@ class Traj(ctypes.Structure):
     _fields_ = [("n_knots", ctypes.c_int64), ("q", ctypes.c_void_p), ("qd", ctypes.c_void_p),
                 ("u", ctypes.c_void_p), ("dqdd", ctypes.c_void_p), ("qdd", ctypes.c_void_p),
                 ("minv", ctypes.c_void_p)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("warps_per_cta", ctypes.c_int), ("lanes_per_knot", ctypes.c_int),
+                ("ragged_warps_per_cta", ctypes.c_int), ("ragged_ctas_per_sm", ctypes.c_int),
+                ("ragged_lanes_per_knot", ctypes.c_int)]
 
 
 class ServerOptions(ctypes.Structure):
@@ -123,6 +133,9 @@ def _declare(L):
         "frg_discrete_jacobians": (st, [vp, i32, vp, vp, ctypes.c_float, vp, vp, vp]),
         "frg_gradient_f64": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp]),
         "frg_verify_f64": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "frg_get_tuning": (st, [vp, ctypes.POINTER(Tuning)]),
+        "frg_set_tuning": (st, [vp, ctypes.POINTER(Tuning)]),
+        "frg_knot_status": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -262,6 +275,16 @@ class Context:
         self._check(lib().frg_autotune(self._h, int(n_knots), ctypes.byref(best)), "frg_autotune")
         return best.value
 
+    def tuning(self):
+        """The tuned launch shapes as a dict (to cache and restore with set_tuning)."""
+        t = Tuning()
+        self._check(lib().frg_get_tuning(self._h, ctypes.byref(t)), "frg_get_tuning")
+        return {f: getattr(t, f) for f, _ in Tuning._fields_}
+
+    def set_tuning(self, tuning):
+        t = Tuning(**{f: int(tuning[f]) for f, _ in Tuning._fields_})
+        self._check(lib().frg_set_tuning(self._h, ctypes.byref(t)), "frg_set_tuning")
+
     # ---------------------------------------------------------- calls
     def gradient(self, n_knots, q, qd, u, dqdd, qdd, minv, stream=None):
         """Plain path on device buffers (addresses, torch tensors)."""
@@ -282,6 +305,11 @@ class Context:
         """Explicit-Euler A [n][14x14], B [n][14x7] from dqdd and minv (device buffers)."""
         self._check(lib().frg_discrete_jacobians(self._h, int(n_knots), _ptr(dqdd), _ptr(minv), float(dt), _ptr(A),
                                                  _ptr(B), _stream_ptr(stream)), "frg_discrete_jacobians")
+
+    def knot_status(self, n_knots, q, qd, u, dqdd, qdd, minv, status, stream=None):
+        """status [n] (uint32/int32 device buffer): KNOT_NONFINITE_INPUT / _OUTPUT flags per knot."""
+        self._check(lib().frg_knot_status(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd),
+                                          _ptr(minv), _ptr(status), _stream_ptr(stream)), "frg_knot_status")
 
     def gradient_f64(self, n_knots, q, qd, u, dqdd, qdd, minv, stream=None):
         """FP64 verification build of the plain path (device double buffers)."""

@@ -231,6 +231,34 @@ void frg_plan_destroy(frg_plan *plan);
 frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s);
 
 /*
+ * The tuned launch shapes of ctx as plain values, so that a caller can keep
+ * the autotuner's choice (in a file, keyed by GPU model) and restore it at
+ * start-up instead of re-tuning.  set validates every field; a shape the GPU
+ * cannot launch fails with FRG_ERR_INVALID_ARGUMENT and changes nothing.
+ */
+typedef struct frg_tuning {
+    int warps_per_cta, lanes_per_knot;                             /* plain launches (contiguous knots) */
+    int ragged_warps_per_cta, ragged_ctas_per_sm, ragged_lanes_per_knot; /* persistent launches */
+} frg_tuning;
+frg_status frg_get_tuning(const frg_ctx *ctx, frg_tuning *out);
+frg_status frg_set_tuning(frg_ctx *ctx, const frg_tuning *tuning);
+
+/*
+ * Per-knot status (DEVICE arrays, asynchronous): status[k] gets
+ * FRG_KNOT_NONFINITE_INPUT if any of knot k's q, qd, u is NaN or infinite, and
+ * FRG_KNOT_NONFINITE_OUTPUT if any of its dqdd, qdd, minv is (outputs may be
+ * NULL: not checked), else 0.  The reference has no such check; its kernel
+ * propagates non-finite values silently.  A non-finite input never spreads to
+ * other knots here (one knot per lane), so the flags locate the bad knots.
+ * One coalesced pass over the arrays, separate from the gradient launch.
+ */
+#define FRG_KNOT_NONFINITE_INPUT 1u
+#define FRG_KNOT_NONFINITE_OUTPUT 2u
+frg_status frg_knot_status(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
+                           const float *dqdd, const float *qdd, const float *minv, uint32_t *status,
+                           frg_stream stream);
+
+/*
  * Continuous-batching server (MPC / iLQR callers).  No counterpart in the
  * reference, whose drivers time one synchronous batch at a time
  * (time_GPU.cu:310-330); it serves the gradient calls of many trajectories as

@@ -109,7 +109,7 @@ static struct {
     pthread_mutex_t mu;
     pthread_cond_t go, done;
     int nthreads, generation, pending, shutdown;
-    int n;
+    int n, given; /* given: q̈ and Minv are inputs (the reference's time_CPU mode) */
     const float *q, *qd, *u;
     float *dqdd, *qdd, *minv;
     worker_t *w;
@@ -123,12 +123,17 @@ static void *worker_main(void *arg) {
         while (!g_pool.shutdown && g_pool.generation == seen) pthread_cond_wait(&g_pool.go, &g_pool.mu);
         if (g_pool.shutdown) { pthread_mutex_unlock(&g_pool.mu); break; }
         seen = g_pool.generation;
-        const int n = g_pool.n, T = g_pool.nthreads;
+        const int n = g_pool.n, T = g_pool.nthreads, given = g_pool.given;
         pthread_mutex_unlock(&g_pool.mu);
         const int per = n / T, k0 = per * w->tid, k1 = (w->tid == T - 1) ? n : per * (w->tid + 1);
-        if (k1 > k0)
+        if (k1 > k0 && given) {
+            for (int k = k0; k < k1; k++)
+                knot_gradient_given_f32(g_pool.q + 7 * k, g_pool.qd + 7 * k, g_pool.qdd + 7 * k,
+                                        g_pool.minv + 49 * k, 0, 0, g_pool.dqdd + 98 * k);
+        } else if (k1 > k0) {
             frg_oracle_gradient_f32(k1 - k0, g_pool.q + 7 * k0, g_pool.qd + 7 * k0, g_pool.u + 7 * k0, NULL, 0, 0,
                                     g_pool.dqdd + 98 * k0, g_pool.qdd + 7 * k0, g_pool.minv + 49 * k0);
+        }
         pthread_mutex_lock(&g_pool.mu);
         if (--g_pool.pending == 0) pthread_cond_signal(&g_pool.done);
         pthread_mutex_unlock(&g_pool.mu);
@@ -162,13 +167,17 @@ static int pool_start(int threads) {
     return 0;
 }
 
-/* Runs `iters` rounds of the FP32 full path over n knots on `threads`
- * persistent workers, DAMPING off / gravity on (the reference's experiment
- * defaults, utils/experiment_helpers.h:19-20).  Returns the wall seconds of
- * all rounds, or a negative value on error.  Not thread-safe. */
-double frg_oracle_time_threaded_f32(int n, const float *q, const float *qd, const float *u, float *dqdd,
-                                    float *qdd, float *minv, int threads, int iters) {
+/* Runs `iters` rounds over n knots on `threads` persistent workers, FP32,
+ * DAMPING off / gravity on (the reference's experiment defaults,
+ * utils/experiment_helpers.h:19-20).  given == 0: the full path (q̈ and Minv
+ * computed and written); given != 0: the reference's time_CPU mode, q̈ and
+ * Minv read from qdd / minv (QDD_MINV_PASSED_IN=true, time_CPU.cpp:30-54).
+ * Returns the wall seconds of all rounds, or a negative value on error.  Not
+ * thread-safe. */
+double frg_oracle_time_threaded_mode_f32(int n, const float *q, const float *qd, const float *u, float *dqdd,
+                                         float *qdd, float *minv, int threads, int iters, int given) {
     if (threads < 1 || n < 0 || iters < 0 || pool_start(threads)) return -1.0;
+    g_pool.given = given != 0;
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
     for (int it = 0; it < iters; it++) {
@@ -182,7 +191,22 @@ double frg_oracle_time_threaded_f32(int n, const float *q, const float *qd, cons
         pthread_mutex_unlock(&g_pool.mu);
     }
     clock_gettime(CLOCK_MONOTONIC, &t1);
+    g_pool.given = 0;
     return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+double frg_oracle_time_threaded_f32(int n, const float *q, const float *qd, const float *u, float *dqdd,
+                                    float *qdd, float *minv, int threads, int iters) {
+    return frg_oracle_time_threaded_mode_f32(n, q, qd, u, dqdd, qdd, minv, threads, iters, 0);
+}
+
+/* The time_CPU-mode gradient alone, single-threaded (for the parity tests). */
+int frg_oracle_gradient_given_f32(int n, const float *q, const float *qd, const float *qdd, const float *minv,
+                                  float *dqdd) {
+    if (n < 0) return 1;
+    for (int k = 0; k < n; k++)
+        knot_gradient_given_f32(&q[7 * k], &qd[7 * k], &qdd[7 * k], &minv[49 * k], 0, 0, &dqdd[98 * k]);
+    return 0;
 }
 
 void frg_oracle_pool_shutdown(void) { pool_stop(); }

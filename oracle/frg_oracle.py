@@ -39,6 +39,10 @@ def _load():
             getattr(L, name).restype = i
         L.frg_oracle_time_threaded_f32.argtypes = [i, vp, vp, vp, vp, vp, vp, i, i]
         L.frg_oracle_time_threaded_f32.restype = ctypes.c_double
+        L.frg_oracle_time_threaded_mode_f32.argtypes = [i, vp, vp, vp, vp, vp, vp, i, i, i]
+        L.frg_oracle_time_threaded_mode_f32.restype = ctypes.c_double
+        L.frg_oracle_gradient_given_f32.argtypes = [i, vp, vp, vp, vp, vp]
+        L.frg_oracle_gradient_given_f32.restype = i
         L.frg_oracle_model_f64.argtypes = [vp, vp, vp]
         L.frg_oracle_pool_shutdown.argtypes = []
         _oracle = L
@@ -118,6 +122,30 @@ def time_threaded_f32(q, qd, u, threads, iters):
     if t < 0:
         raise RuntimeError("oracle thread pool failed")
     return t, (dqdd, qdd, minv)
+
+
+def time_threaded_given_f32(q, qd, u, threads, iters):
+    """Wall seconds of `iters` rounds of the reference's time_CPU mode: q̈ and
+    Minv precomputed (untimed) and passed in, the gradient timed."""
+    q, qd, u = (np.ascontiguousarray(x, dtype=np.float32) for x in (q, qd, u))
+    n = q.shape[0]
+    dqdd, qdd, minv = gradient_f32(q, qd, u)
+    L = _load()
+    t = L.frg_oracle_time_threaded_mode_f32(n, q.ctypes.data, qd.ctypes.data, u.ctypes.data, dqdd.ctypes.data,
+                                            qdd.ctypes.data, minv.ctypes.data, int(threads), int(iters), 1)
+    if t < 0:
+        raise RuntimeError("oracle thread pool failed")
+    return t, (dqdd, qdd, minv)
+
+
+def gradient_given_f32(q, qd, qdd, minv):
+    """dqdd [n,98] from q, qd and the given q̈ [n,7], Minv [n,49] (time_CPU mode)."""
+    q, qd, qdd, minv = (np.ascontiguousarray(x, dtype=np.float32) for x in (q, qd, qdd, minv))
+    n = q.shape[0]
+    dqdd = np.zeros((n, 98), np.float32)
+    _load().frg_oracle_gradient_given_f32(n, q.ctypes.data, qd.ctypes.data, qdd.ctypes.data, minv.ctypes.data,
+                                          dqdd.ctypes.data)
+    return dqdd
 
 
 def shutdown_pool():

@@ -357,3 +357,25 @@ static void FN(knot_gradient)(const REAL *q, const REAL *qd, const REAL *u, cons
     for (int cc = 0; cc < NJ; cc++)
         for (int r = 0; r < NJ; r++) minv_dense[r + NJ * cc] = r <= cc ? Minv[r + NJ * cc] : Minv[cc + NJ * r];
 }
+
+/* The reference's time_CPU mode, QDD_MINV_PASSED_IN=true (dynamicsGradient.h:
+ * 869-897 with the flag set, :925-934): q̈ and Minv (dense) come in, RNEA runs
+ * once with that q̈, then d tau and dqdd = -Minv [d tau/dq | d tau/dqd]. */
+static void FN(knot_gradient_given)(const REAL *q, const REAL *qd, const REAL *qdd, const REAL *minv_dense,
+                                    int damping, int mpc, REAL *dqdd) {
+    REAL sq[NJ], cq[NJ], X[NJ * 36], I[NJ * 36];
+    for (int k = 0; k < NJ; k++) { sq[k] = (REAL)sin(q[k]); cq[k] = (REAL)cos(q[k]); }
+    FN(model_transforms)(X, sq, cq);
+    FN(model_inertias)(I);
+    REAL v[NJ * 6], a[NJ * 6], f[NJ * 6];
+    FN(rnea_forward)(v, a, f, X, I, qd, qdd, NULL, mpc);
+    FN(rnea_backward)(NULL, f, X);
+    REAL cdu[2 * NJ * NJ];
+    FN(dtau_columns)(cdu, &cdu[NJ * NJ], v, a, f, X, I, qd, damping);
+    for (int col = 0; col < 2 * NJ; col++)
+        for (int r = 0; r < NJ; r++) {
+            REAL acc = 0;
+            for (int k = 0; k < NJ; k++) acc += (r <= k ? minv_dense[r + NJ * k] : minv_dense[k + NJ * r]) * cdu[k + NJ * col];
+            dqdd[r + NJ * col] = -acc;
+        }
+}

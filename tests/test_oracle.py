@@ -89,3 +89,14 @@ def test_threaded_driver_matches_serial():
     d2, q2, m2 = frg_oracle.gradient_f32(q, qd, u)
     assert t > 0
     assert np.array_equal(d, d2) and np.array_equal(qq, q2) and np.array_equal(m, m2)
+
+
+def test_time_cpu_mode_matches_full_path():
+    """The reference's time_CPU mode (q̈ and Minv passed in) gives the full
+    path's dqdd bit for bit when fed the full path's own q̈ and Minv; the
+    threaded driver in that mode agrees with the serial call."""
+    q, qd, u = frg.sample_knots(130, seed=8)
+    d, qq, m = frg_oracle.gradient_f32(q, qd, u)
+    assert np.array_equal(frg_oracle.gradient_given_f32(q, qd, qq, m), d)
+    t, (d3, q3, m3) = frg_oracle.time_threaded_given_f32(q, qd, u, threads=3, iters=2)
+    assert t > 0 and np.array_equal(d3, d) and np.array_equal(q3, qq) and np.array_equal(m3, m)
