@@ -271,7 +271,9 @@ frg_status frg_knot_status(frg_ctx *ctx, int n_knots, const float *q, const floa
  *  - a dispatcher thread folds all ready calls into the next persistent
  *    launch (up to max_batch_knots) while up to max_inflight earlier launches
  *    still run, each on its own stream;
- *  - results of a call are bit-identical alone or batched with any others.
+ *  - results of a call are bit-identical alone or batched with any others:
+ *    every knot's arithmetic is the same in both thread mappings, whichever
+ *    the batch size selects.
  * One call per trajectory may be in flight; submit copies the inputs.
  */
 typedef struct frg_server frg_server;
@@ -283,7 +285,8 @@ typedef struct frg_server_options {
     int warps_per_cta;    /* launch shape of larger server launches, 0 = the context's */
     int ctas_per_sm;
     int latency_mapping_max_knots; /* batches up to this many knots use the
-                                      8-lanes-per-knot mapping (default 4096) */
+                                      8-lanes-per-knot mapping (default 4096;
+                                      0: one lane per knot for every batch) */
 } frg_server_options;
 
 typedef struct frg_request_info {

@@ -171,3 +171,20 @@ def test_host_call_pinned_zero_copy_equals_staged(n, lanes, offset):
     finally:
         for ptr, _, _ in bufs.values():
             L.frg_host_free(ptr)
+
+
+@pytest.mark.parametrize("damping,mpc", MODES)
+def test_thread_mappings_give_identical_bits(damping, mpc):
+    """Both thread mappings perform the same operations in the same order for
+    every knot (the latency mapping only spreads the columns over lanes), so
+    their results agree bit for bit, here on 20,000 knots."""
+    n = 20000
+    q, qd, u = frg.sample_knots(n, seed=500 + 2 * damping + mpc)
+    with frg.Context(vel_damping=damping, mpc_mode=mpc) as ctx:
+        ctx.set_lanes_per_knot(1)
+        a = ctx.gradient_host(q, qd, u)
+        ctx.set_lanes_per_knot(8)
+        b = ctx.gradient_host(q, qd, u)
+    for name, x, y in zip(("dqdd", "qdd", "minv"), a, b):
+        diff = np.count_nonzero(x != y)
+        assert diff == 0, f"{name}: {diff} values differ, max {max_err(x, y):.2e}"

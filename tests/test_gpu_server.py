@@ -152,3 +152,24 @@ def test_server_argument_errors():
         srv.wait(rid)
         assert srv.poll(123456)[0] == 8
         assert srv.stats()["rejected"] == 1
+
+
+def test_thread_mapping_threshold_keeps_bits():
+    """A small call is served with 8 lanes per knot by default and with one
+    lane per knot when latency_mapping_max_knots = 0; both give the plain
+    path's bits, so a call's result does not depend on the size of the batch
+    it lands in."""
+    q, qd, u = knots(48, 5)
+    with frg.Context() as ctx:
+        ctx.set_lanes_per_knot(1)
+        plain = ctx.gradient_host(q, qd, u)
+        results = []
+        for threshold in (0, None):
+            with frg.Server(ctx, latency_mapping_max_knots=threshold) as srv:
+                st, rid = srv.submit(3, q, qd, u)
+                st, info = srv.wait(rid, timeout_us=10_000_000)
+                assert st == 0 and info.status == 0
+                results.append(frg.Server.results(info))
+    for res in results:
+        for a, b in zip(res, plain):
+            assert np.array_equal(a, b)
