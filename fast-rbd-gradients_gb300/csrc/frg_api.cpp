@@ -15,6 +15,7 @@
 
 #include "frg_internal.h"
 #include "frg_kernels.cuh"
+#include "frg_model_select.h"
 
 using frg::LaunchShape;
 using frg::Segment;
@@ -155,6 +156,8 @@ void frg_options_default(frg_options *opt) {
     opt->ctas_per_sm = 0;
     opt->lanes_per_knot = 0;
 }
+
+const char *frg_model_name(void) { return FRG_MODEL_NAME; }
 
 const char *frg_status_string(frg_status s) {
     switch (s) {

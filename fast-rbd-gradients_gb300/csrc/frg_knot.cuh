@@ -201,15 +201,32 @@ __device__ __forceinline__ void rotz_gen(real G[3][3], const real N[3][3], real 
     }
 }
 
-// O = F^T G F:  O[i][j] = s_i s_j G[p_i][p_j]
+// O = F^T G F:  O[i][j] = s_i s_j G[p_i][p_j] for a signed permutation F,
+// else the general product (structural zeros of F dropped at compile time).
 template <int k> __device__ __forceinline__ void perm_FT_G_F(real O[3][3], const real G[3][3]) {
     using J = Joint<k>;
-    constexpr int p[3] = {J::p0, J::p1, J::p2};
-    constexpr real sg[3] = {J::s0, J::s1, J::s2};
+    if constexpr (J::perm) {
+        constexpr int p[3] = {J::p0, J::p1, J::p2};
+        constexpr real sg[3] = {J::s0, J::s1, J::s2};
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+        for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int j = 0; j < 3; j++) O[i][j] = (sg[i] * sg[j]) * G[p[i]][p[j]];
+            for (int j = 0; j < 3; j++) O[i][j] = (sg[i] * sg[j]) * G[p[i]][p[j]];
+    } else {
+        real GF[3][3];  // G F: row a of G F is F^T applied to row a of G
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const real row[3] = {G[a][0], G[a][1], G[a][2]};
+            mul_FT<k>(GF[a], row);
+        }
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const real col[3] = {GF[0][j], GF[1][j], GF[2][j]};
+            real o[3];
+            mul_FT<k>(o, col);  // O[i][j] = sum_a F[a][i] (G F)[a][j]
+            O[0][j] = o[0]; O[1][j] = o[1]; O[2][j] = o[2];
+        }
+    }
 }
 
 // X_k^T [A B; B^T M] X_k for the joint transform X_k = [E 0; -E r^ E].
@@ -243,7 +260,7 @@ __device__ __forceinline__ void congruence(real Ao[3][3], real Bo[3][3], real Mo
         Ao[1][1] = fmaR(t, Bt[1][0], fmaR(t, Bo[1][0], At[1][1]));
         Ao[1][2] = fmaR(t, Bt[2][0], At[1][2]);
         Ao[2][2] = At[2][2];
-    } else {
+    } else if constexpr (J::axis == 1) {
         // r^ = [0 0 t; 0 0 0; -t 0 0]
 #pragma unroll
         for (int j = 0; j < 3; j++) {
@@ -259,6 +276,31 @@ __device__ __forceinline__ void congruence(real Ao[3][3], real Bo[3][3], real Mo
         Ao[1][1] = At[1][1];
         Ao[1][2] = fmaR(-t, Bo[1][0], At[1][2]);
         Ao[2][2] = fmaR(-t, Bt[2][0], fmaR(-t, Bo[2][0], At[2][2]));
+    } else {
+        // other origins: r^ = [0 -r2 r1; r2 0 -r0; -r1 r0 0]
+        constexpr real rh[3][3] = {{0, -J::r2, J::r1}, {J::r2, 0, -J::r0}, {-J::r1, J::r0, 0}};
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                real acc = Bt[i][j];
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+                    if (rh[i][a] != real(0)) acc = fmaR(rh[i][a], Mo[a][j], acc);
+                Bo[i][j] = acc;  // Bt + r^ Mt
+            }
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = i; j < 3; j++) {
+                real acc = At[i][j];
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    if (rh[i][a] != real(0)) acc = fmaR(rh[i][a], Bt[j][a], acc);   // + r^ Bt^T
+                    if (rh[a][j] != real(0)) acc = fmaR(-rh[a][j], Bo[i][a], acc);  // - B' r^
+                }
+                Ao[i][j] = acc;
+            }
     }
     Ao[1][0] = Ao[0][1]; Ao[2][0] = Ao[0][2]; Ao[2][1] = Ao[1][2];
 }
@@ -450,6 +492,8 @@ __device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const real
                 const real g[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, kGravity};
                 xmotion<0>(a, g, cq[0], sq[0]);
             }
+            if constexpr (!kDqColumn0Zero)  // X_0 a_base, read by d tau / dq column 0
+                ws->link[kSlotsPerLink * 0 + 3][lane] = make_real4(a[0], a[1], a[3], a[4]);
             a[2] += qdd[0];
         } else {
             real xa[6];
@@ -641,12 +685,15 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
         __syncwarp();
     }
 
-    // d qdd / dq: columns 0..6 (column 0 is identically zero for this model:
-    // the base joint axis is parallel to gravity, as dynamicsGradient.h:797-813 uses)
+    // d qdd / dq: columns 0..6 (column 0 is identically zero when the base
+    // joint axis is parallel to gravity, as for the iiwa and as
+    // dynamicsGradient.h:797-813 uses; other models compute it)
+    if constexpr (kDqColumn0Zero) {
 #pragma unroll
-    for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r] = 0.0f;
+        for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r] = 0.0f;
+    }
 #pragma unroll 1
-    for (int c = 1; c < kJoints; c++) {
+    for (int c = kDqColumn0Zero ? 1 : 0; c < kJoints; c++) {
         real dtau[7], out[7];
         dtau_column<true, DAMP>(ws, lane, c, qd, sq, cq, dtau);
         minv_times(out, Mi, dtau);

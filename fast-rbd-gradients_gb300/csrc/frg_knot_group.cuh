@@ -49,7 +49,7 @@ __device__ __forceinline__ void g_dtau_column(const GroupSmem *gs, int ks, int c
     float dv[6] = {0, 0, 0, 0, 0, 0}, da[6] = {0, 0, 0, 0, 0, 0};
     static_for<0, kJoints>([&](auto K) {
         constexpr int k = decltype(K)::value;
-        if constexpr (QSIDE && k == 0) {
+        if constexpr (QSIDE && k == 0 && kDqColumn0Zero) {
 #pragma unroll
             for (int i = 0; i < 6; i++) df[0][i] = 0.0f;  // dq column 0 is zero; c >= 1 on this side
             return;
@@ -293,6 +293,8 @@ __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const Kno
                     const float g6[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, kGravity};
                     xmotion<0>(a, g6, cq[0], sq[0]);
                 }
+                if constexpr (!kDqColumn0Zero)  // X_0 a_base, read by d tau / dq column 0
+                    g_sts<0>(gs, ks, 3, make_float4(a[0], a[1], a[3], a[4]));
                 a[2] += qdd[0];
             } else {
                 float xa[6];
@@ -319,7 +321,8 @@ __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const Kno
     }
     __syncwarp();
 
-    // tangent columns: dqd column g and dq column 7 - g (none for g = 0 / 7)
+    // tangent columns: dqd column g and dq column 7 - g (none for g = 7 / 0;
+    // lane 7's dq column 0 is computed unless the model makes it vanish)
     float mrow[7][7];
 #pragma unroll
     for (int r = 0; r < 7; r++)
@@ -350,7 +353,7 @@ __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const Kno
                 for (int k = 0; k < 7; k++) acc = fmaf(mrow[r][k], dtau[k], acc);
                 gs->out[ks][7 * cq_col + r] = -acc;
             }
-        } else {
+        } else if constexpr (kDqColumn0Zero) {
 #pragma unroll
             for (int r = 0; r < 7; r++) gs->out[ks][r] = 0.0f;  // dq column 0 is identically zero
         }

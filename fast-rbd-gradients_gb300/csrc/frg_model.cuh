@@ -55,19 +55,24 @@ template <int B, int E, typename F> __device__ __forceinline__ void static_for_d
 
 // ------------------------------------------------------------------ model ---
 
-// Link inertial data of utils/iiwa_14.urdf (iiwa_link_1..7): inertia at the
-// COM (xx xy xz yy yz zz), COM position (x y z), mass.  The same numbers as the
-// reference's l0..l6 constants (dynamicsGradient.h:127-202).
+// The robot comes from one header of tables (written by frg/urdf.py from a
+// URDF): the build defines FRG_MODEL_TABLES to select another robot; the
+// default is the iiwa_14 of utils/iiwa_14.urdf, the reference's only model.
+#include "frg_model_select.h"
+
+// Link inertia at the COM (xx xy xz yy yz zz), COM position (x y z), mass, in
+// the link frame.  For the iiwa these are the reference's l0..l6 constants
+// (dynamicsGradient.h:127-202).
 struct LinkInertial { double ixx, ixy, ixz, iyy, iyz, izz, cx, cy, cz, m; };
-constexpr LinkInertial kLinks[kJoints] = {
-    {0.121, 0.0, 0.0, 0.116, -0.021, 0.0175, 0.0, -0.03, 0.12, 5.76},
-    {0.0638, 0.0001, 0.00008, 0.0416, 0.0157, 0.0331, 0.0003, 0.059, 0.042, 6.35},
-    {0.0873, 0.0, 0.0, 0.083, 0.014, 0.0108, 0.0, 0.03, 0.13, 3.5},
-    {0.0368, 0.0, 0.0, 0.02045, 0.008, 0.02171, 0.0, 0.067, 0.034, 3.5},
-    {0.0318, 0.000007, 0.000027, 0.028916, 0.005586, 0.006, 0.0001, 0.021, 0.076, 3.5},
-    {0.0049, 0.0, 0.0, 0.0047, 0.0, 0.0036, 0.0, 0.0006, 0.0004, 1.8},
-    {0.0055, 0.0, 0.0, 0.0055, 0.0, 0.005, 0.0, 0.0, 0.02, 1.2},
-};
+constexpr LinkInertial kLinks[kJoints] = FRG_MODEL_LINK_INERTIAL;
+// Joint frames: F = R^T of the joint frame in its parent (column-major), the
+// joint origin r in the parent frame (the iiwa's tz_j1..ty_j7,
+// dynamicsGradient.h:223-229).
+constexpr double kModelF[kJoints][9] = FRG_MODEL_JOINT_F;
+constexpr double kModelOrigin[kJoints][3] = FRG_MODEL_JOINT_ORIGIN;
+// Column 0 of d tau / dq vanishes identically when gravity lies along the
+// first joint's axis (the iiwa; the reference relies on it at :797-813).
+constexpr bool kDqColumn0Zero = FRG_MODEL_DQ_COLUMN0_ZERO != 0;
 
 // Spatial inertia about the joint origin: rotational block Ibar = Icom +
 // m (|c|^2 1 - c c^T) (the parallel-axis shift buildI6x6 applies,
@@ -84,73 +89,135 @@ template <int k> struct Link {
     static constexpr real m = real(L.m);
 };
 
-// Joint frames (utils/iiwa_14.urdf iiwa_joint_1..7 <origin>).  F maps w to
-// (F w)[p_i] = s_i w_i; axis/t give r = t e_axis (axis 1 = y, 2 = z).
-//   rpy (0,0,0):                 p = {0,1,2}, s = {+,+,+}
-//   rpy (pi/2,0,pi), (-pi/2,pi,0): p = {0,2,1}, s = {-,+,+}   w -> (-w0, w2, w1)
-//   rpy (pi/2,0,0):              p = {0,2,1}, s = {+,-,+}   w -> (w0, w2, -w1)
-// Translations as tz_j1..ty_j7, dynamicsGradient.h:223-229.
-template <int k> struct Joint;
-template <> struct Joint<0> { static constexpr int p0 = 0, p1 = 1, p2 = 2; static constexpr real s0 = 1, s1 = 1, s2 = 1; static constexpr int axis = 2; static constexpr real t = real(0.1575); };
-template <> struct Joint<1> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 2; static constexpr real t = real(0.2025); };
-template <> struct Joint<2> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr real t = real(0.2045); };
-template <> struct Joint<3> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = 1, s1 = -1, s2 = 1; static constexpr int axis = 2; static constexpr real t = real(0.2155); };
-template <> struct Joint<4> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr real t = real(0.1845); };
-template <> struct Joint<5> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = 1, s1 = -1, s2 = 1; static constexpr int axis = 2; static constexpr real t = real(0.2155); };
-template <> struct Joint<6> { static constexpr int p0 = 0, p1 = 2, p2 = 1; static constexpr real s0 = -1, s1 = 1, s2 = 1; static constexpr int axis = 1; static constexpr real t = real(0.081); };
+// Structure of each joint frame, found at compile time.  A signed
+// permutation F (frames in multiples of pi/2, as every iiwa joint) maps w to
+// (F w)[p_i] = s_i w_i; an origin on one axis (every iiwa joint) is
+// r = t e_axis.  Other frames take the general 3x3 / cross-product forms.
+//   iiwa rpy (0,0,0):                 p = {0,1,2}, s = {+,+,+}
+//   iiwa rpy (pi/2,0,pi), (-pi/2,pi,0): p = {0,2,1}, s = {-,+,+}   w -> (-w0, w2, w1)
+//   iiwa rpy (pi/2,0,0):              p = {0,2,1}, s = {+,-,+}   w -> (w0, w2, -w1)
+__host__ __device__ constexpr double kF(int k, int r, int c) { return kModelF[k][r + 3 * c]; }
+__host__ __device__ constexpr int perm_row(int k, int c) {
+    int row = -1, n = 0;
+    for (int r = 0; r < 3; r++)
+        if (kF(k, r, c) != 0.0) { row = r; n++; }
+    return (n == 1 && (kF(k, row, c) == 1.0 || kF(k, row, c) == -1.0)) ? row : -1;
+}
+__host__ __device__ constexpr bool signed_perm(int k) {
+    const int a = perm_row(k, 0), b = perm_row(k, 1), c = perm_row(k, 2);
+    return a >= 0 && b >= 0 && c >= 0 && a != b && b != c && a != c;
+}
+__host__ __device__ constexpr int origin_axis(int k) {  // 0..2: one nonzero component; 3: r = 0; -1: general
+    int axis = 3, n = 0;
+    for (int i = 0; i < 3; i++)
+        if (kModelOrigin[k][i] != 0.0) { axis = i; n++; }
+    return n <= 1 ? axis : -1;
+}
+template <int k> struct Joint {
+    static constexpr bool perm = signed_perm(k);
+    static constexpr int p0 = perm ? perm_row(k, 0) : 0, p1 = perm ? perm_row(k, 1) : 1, p2 = perm ? perm_row(k, 2) : 2;
+    static constexpr real s0 = real(kF(k, p0, 0)), s1 = real(kF(k, p1, 1)), s2 = real(kF(k, p2, 2));
+    static constexpr int axis = origin_axis(k);
+    static constexpr real t = (axis >= 0 && axis < 3) ? real(kModelOrigin[k][axis]) : real(0);
+    static constexpr real r0 = real(kModelOrigin[k][0]), r1 = real(kModelOrigin[k][1]), r2 = real(kModelOrigin[k][2]);
+};
+
+// acc += K x for a compile-time K, dropped when K == 0
+template <typename KC> __device__ __forceinline__ void fma_const(real &acc, KC, real x) {
+    if constexpr (KC::value != 0.0) acc = fmaR(real(KC::value), x, acc);
+}
+template <int k, int r, int c> struct FEntry { static constexpr double value = kModelF[k][r + 3 * c]; };
 
 // ------------------------------------------------------- 3-vector pieces ---
+
+// F w for joint k (general frames)
+template <int k> __device__ __forceinline__ void mul_F(real o[3], const real w[3]) {
+    static_for<0, 3>([&](auto R) {
+        constexpr int r = decltype(R)::value;
+        real acc = real(0);
+        fma_const(acc, FEntry<k, r, 0>{}, w[0]);
+        fma_const(acc, FEntry<k, r, 1>{}, w[1]);
+        fma_const(acc, FEntry<k, r, 2>{}, w[2]);
+        o[r] = acc;
+    });
+}
+// F^T w for joint k (general frames)
+template <int k> __device__ __forceinline__ void mul_FT(real o[3], const real w[3]) {
+    static_for<0, 3>([&](auto C) {
+        constexpr int c = decltype(C)::value;
+        real acc = real(0);
+        fma_const(acc, FEntry<k, 0, c>{}, w[0]);
+        fma_const(acc, FEntry<k, 1, c>{}, w[1]);
+        fma_const(acc, FEntry<k, 2, c>{}, w[2]);
+        o[c] = acc;
+    });
+}
 
 // E w = Rz(q)^T (F w)
 template <int k> __device__ __forceinline__ void rot_E(real o[3], const real w[3], real c, real s) {
     using J = Joint<k>;
     real fw[3];
-    fw[J::p0] = J::s0 * w[0];
-    fw[J::p1] = J::s1 * w[1];
-    fw[J::p2] = J::s2 * w[2];
+    if constexpr (J::perm) {
+        fw[J::p0] = J::s0 * w[0];
+        fw[J::p1] = J::s1 * w[1];
+        fw[J::p2] = J::s2 * w[2];
+    } else {
+        mul_F<k>(fw, w);
+    }
     o[0] = fmaR(c, fw[0], s * fw[1]);
     o[1] = fmaR(c, fw[1], -s * fw[0]);
     o[2] = fw[2];
 }
 
-// E^T w = F^T (Rz(q) w),  (F^T x)_i = s_i x[p_i]
+// E^T w = F^T (Rz(q) w),  (F^T x)_i = s_i x[p_i] for a signed permutation
 template <int k> __device__ __forceinline__ void rot_ET(real o[3], const real w[3], real c, real s) {
     using J = Joint<k>;
     real x[3];
     x[0] = fmaR(c, w[0], -s * w[1]);
     x[1] = fmaR(c, w[1], s * w[0]);
     x[2] = w[2];
-    o[0] = J::s0 * x[J::p0];
-    o[1] = J::s1 * x[J::p1];
-    o[2] = J::s2 * x[J::p2];
+    if constexpr (J::perm) {
+        o[0] = J::s0 * x[J::p0];
+        o[1] = J::s1 * x[J::p1];
+        o[2] = J::s2 * x[J::p2];
+    } else {
+        mul_FT<k>(o, x);
+    }
 }
 
-// o = u - r x w  (r = t e_axis)
-template <int k> __device__ __forceinline__ void sub_r_cross(real o[3], const real u[3], const real w[3]) {
+// o = u + sgn (r x w)  (sgn = -1: u - r x w)
+template <int k, int sgn> __device__ __forceinline__ void r_cross_acc(real o[3], const real u[3], const real w[3]) {
     using J = Joint<k>;
+    constexpr real g = real(sgn);
     if constexpr (J::axis == 2) {  // r x w = (-t w1, t w0, 0)
-        o[0] = fmaR(J::t, w[1], u[0]);
-        o[1] = fmaR(-J::t, w[0], u[1]);
+        o[0] = fmaR(-g * J::t, w[1], u[0]);
+        o[1] = fmaR(g * J::t, w[0], u[1]);
         o[2] = u[2];
-    } else {  // axis y: r x w = (t w2, 0, -t w0)
-        o[0] = fmaR(-J::t, w[2], u[0]);
+    } else if constexpr (J::axis == 1) {  // r x w = (t w2, 0, -t w0)
+        o[0] = fmaR(g * J::t, w[2], u[0]);
         o[1] = u[1];
-        o[2] = fmaR(J::t, w[0], u[2]);
+        o[2] = fmaR(-g * J::t, w[0], u[2]);
+    } else if constexpr (J::axis == 0) {  // r x w = (0, -t w2, t w1)
+        o[0] = u[0];
+        o[1] = fmaR(-g * J::t, w[2], u[1]);
+        o[2] = fmaR(g * J::t, w[1], u[2]);
+    } else if constexpr (J::axis == 3) {  // r = 0
+        o[0] = u[0]; o[1] = u[1]; o[2] = u[2];
+    } else {  // r x w = (r1 w2 - r2 w1, r2 w0 - r0 w2, r0 w1 - r1 w0)
+        o[0] = fmaR(-g * J::r2, w[1], fmaR(g * J::r1, w[2], u[0]));
+        o[1] = fmaR(-g * J::r0, w[2], fmaR(g * J::r2, w[0], u[1]));
+        o[2] = fmaR(-g * J::r1, w[0], fmaR(g * J::r0, w[1], u[2]));
     }
+}
+
+// o = u - r x w
+template <int k> __device__ __forceinline__ void sub_r_cross(real o[3], const real u[3], const real w[3]) {
+    r_cross_acc<k, -1>(o, u, w);
 }
 
 // o = u + r x w
 template <int k> __device__ __forceinline__ void add_r_cross(real o[3], const real u[3], const real w[3]) {
-    using J = Joint<k>;
-    if constexpr (J::axis == 2) {
-        o[0] = fmaR(-J::t, w[1], u[0]);
-        o[1] = fmaR(J::t, w[0], u[1]);
-        o[2] = u[2];
-    } else {
-        o[0] = fmaR(J::t, w[2], u[0]);
-        o[1] = u[1];
-        o[2] = fmaR(-J::t, w[0], u[2]);
-    }
+    r_cross_acc<k, 1>(o, u, w);
 }
 
 // ------------------------------------------------------- spatial vectors ---

@@ -17,4 +17,5 @@ from .native import (  # noqa: F401
     Server,
     forward_dynamics_gradient,
     lib,
+    model_name,
 )

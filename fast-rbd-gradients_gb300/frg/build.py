@@ -5,6 +5,10 @@
 Translation units compile in parallel into fast-rbd-gradients_gb300/_build/;
 the link uses the shared CUDA runtime so that the library and PyTorch share one
 runtime (and one primary context) when both are loaded.
+
+The robot is compiled in: the iiwa_14 by default, another 7-joint serial arm
+from a tables header written by frg/urdf.py when FRG_MODEL_TABLES names it
+(in-tree build), or build_model(tables, out_dir) for a library of its own.
 """
 import concurrent.futures
 import os
@@ -48,17 +52,27 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _model_flags(tables):
+    return [f'-DFRG_MODEL_TABLES="{os.path.abspath(tables)}"'] if tables else []
+
+
 def build(force=False, verbose=False, ptxas_info=False):
     """Compile and link libfrg.so if any source or header changed; returns its path."""
     nvcc = _nvcc()
     os.makedirs(BUILD_DIR, exist_ok=True)
-    hdrs = _headers()
+    tables = os.environ.get("FRG_MODEL_TABLES") or None
+    stamp = os.path.join(BUILD_DIR, "model.txt")
+    model_id = os.path.abspath(tables) if tables else "default"
+    if not os.path.exists(stamp) or open(stamp).read() != model_id:
+        force = True  # another robot: every translation unit changes
+    hdrs = _headers() + ([tables] if tables else [])
     jobs = []
     for src in sources():
         obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
         if force or _stale(obj, [src] + hdrs):
             extra = ["-Xptxas", "-v"] if (ptxas_info and src.endswith(".cu")) else []
-            jobs.append((src, obj, [nvcc] + ARCH_FLAGS + COMMON + extra + ["-c", src, "-o", obj]))
+            jobs.append((src, obj, [nvcc] + ARCH_FLAGS + COMMON + _model_flags(tables) + extra +
+                         ["-c", src, "-o", obj]))
 
     def run(job):
         src, obj, cmd = job
@@ -83,8 +97,38 @@ def build(force=False, verbose=False, ptxas_info=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of libfrg.so failed:\n{r.stdout}\n{r.stderr}")
+    with open(stamp, "w") as f:
+        f.write(model_id)
     build_host_tools(nvcc, force, verbose)
     return LIB_PATH
+
+
+def build_model(tables, out_dir, verbose=False):
+    """libfrg.so for the robot of a tables header (frg/urdf.py) in out_dir,
+    beside the in-tree library; returns its path."""
+    nvcc = _nvcc()
+    obj_dir = os.path.join(out_dir, "obj")
+    os.makedirs(obj_dir, exist_ok=True)
+    jobs = [(src, os.path.join(obj_dir, os.path.basename(src) + ".o")) for src in sources()]
+
+    def run(job):
+        src, obj = job
+        cmd = [nvcc] + ARCH_FLAGS + COMMON + _model_flags(tables) + ["-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+        list(ex.map(run, jobs))
+    lib = os.path.join(out_dir, "libfrg.so")
+    cmd = [nvcc] + ARCH_FLAGS + ["-shared", "-cudart", "shared", "-o", lib] + [o for _, o in jobs] + [
+        "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link of {lib} failed:\n{r.stdout}\n{r.stderr}")
+    return lib
 
 
 def build_host_tools(nvcc, force=False, verbose=False):

@@ -35,7 +35,7 @@ EXPORTED = (
     "frg_server_create", "frg_server_destroy", "frg_server_submit", "frg_server_poll", "frg_server_wait",
     "frg_server_wait_any", "frg_server_release", "frg_server_get_stats", "frg_gradient_fext",
     "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64", "frg_get_tuning",
-    "frg_set_tuning", "frg_knot_status",
+    "frg_set_tuning", "frg_knot_status", "frg_model_name",
 )
 
 KNOT_NONFINITE_INPUT = 1
@@ -136,6 +136,7 @@ def _declare(L):
         "frg_get_tuning": (st, [vp, ctypes.POINTER(Tuning)]),
         "frg_set_tuning": (st, [vp, ctypes.POINTER(Tuning)]),
         "frg_knot_status": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "frg_model_name": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -154,6 +155,11 @@ def lib():
         _declare(L)
         _lib = L
     return _lib
+
+
+def model_name():
+    """Name of the robot compiled into the loaded library."""
+    return lib().frg_model_name().decode()
 
 
 def _ptr(x):

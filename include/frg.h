@@ -79,6 +79,11 @@ typedef struct frg_options {
 
 void frg_options_default(frg_options *opt);
 const char *frg_status_string(frg_status s);
+/* The robot this library was built for: "iiwa_14" (the default, the
+ * reference's model, code-generated there at helpers_CPU/dynamicsGradient.h:
+ * 124-229) or the name in the tables header frg/urdf.py wrote from another
+ * URDF of a 7-joint serial arm. */
+const char *frg_model_name(void);
 
 /* Creates a context on opt->device (NULL opt = defaults). */
 frg_status frg_create(frg_ctx **out, const frg_options *opt);

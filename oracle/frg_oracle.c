@@ -20,39 +20,24 @@
 /* g, as the reference's GRAVITY default (dynamicsGradient.h:7-9). */
 static const double kGravity = 9.81;
 
-/* Link inertial data from utils/iiwa_14.urdf (links iiwa_link_1..7, lines
- * 31-37, 47-53, 63-69, 79-85, 95-101, 111-119, 129-137): the same constants
- * the reference code-generates at dynamicsGradient.h:127-202.  Columns:
- * Ixx Ixy Ixz Iyy Iyz Izz (at the COM), COM x y z, mass. */
-static const double kLinkInertial[7][10] = {
-    {0.121, 0.0, 0.0, 0.116, -0.021, 0.0175, 0.0, -0.03, 0.12, 5.76},
-    {0.0638, 0.0001, 0.00008, 0.0416, 0.0157, 0.0331, 0.0003, 0.059, 0.042, 6.35},
-    {0.0873, 0.0, 0.0, 0.083, 0.014, 0.0108, 0.0, 0.03, 0.13, 3.5},
-    {0.0368, 0.0, 0.0, 0.02045, 0.008, 0.02171, 0.0, 0.067, 0.034, 3.5},
-    {0.0318, 0.000007, 0.000027, 0.028916, 0.005586, 0.006, 0.0001, 0.021, 0.076, 3.5},
-    {0.0049, 0.0, 0.0, 0.0047, 0.0, 0.0036, 0.0, 0.0006, 0.0004, 1.8},
-    {0.0055, 0.0, 0.0, 0.0055, 0.0, 0.005, 0.0, 0.0, 0.02, 1.2},
-};
-
-/* Joint frames from utils/iiwa_14.urdf (iiwa_joint_1..7 <origin>, lines 26,
- * 42, 58, 74, 90, 106, 124): F = R(rpy)^T as a column-major signed
- * permutation, and the joint origin xyz in the parent frame.  rpy (0,0,0) ->
- * identity; (pi/2,0,pi) and (-pi/2,pi,0) -> w |-> (-w0, w2, w1);
- * (pi/2,0,0) -> w |-> (w0, w2, -w1).  Same translations as the reference's
- * tz_j1..ty_j7 (dynamicsGradient.h:223-229). */
-static const double kJointFT[7][9] = {
-    {1, 0, 0, 0, 1, 0, 0, 0, 1},
-    {-1, 0, 0, 0, 0, 1, 0, 1, 0},
-    {-1, 0, 0, 0, 0, 1, 0, 1, 0},
-    {1, 0, 0, 0, 0, -1, 0, 1, 0},
-    {-1, 0, 0, 0, 0, 1, 0, 1, 0},
-    {1, 0, 0, 0, 0, -1, 0, 1, 0},
-    {-1, 0, 0, 0, 0, 1, 0, 1, 0},
-};
-static const double kJointOrigin[7][3] = {
-    {0, 0, 0.1575}, {0, 0, 0.2025}, {0, 0.2045, 0}, {0, 0, 0.2155},
-    {0, 0.1845, 0}, {0, 0, 0.2155}, {0, 0.081, 0},
-};
+/* The model: the same tables the kernels compile (FRG_MODEL_TABLES selects a
+ * generated robot; default the iiwa_14 of utils/iiwa_14.urdf).
+ *  - link inertial (Ixx Ixy Ixz Iyy Iyz Izz at the COM, COM x y z, mass): for
+ *    the iiwa the constants the reference code-generates at
+ *    dynamicsGradient.h:127-202 (urdf lines 31-37, 47-53, ..., 129-137);
+ *  - F = R(rpy)^T of each joint frame, column-major (for the iiwa signed
+ *    permutations: rpy (0,0,0) -> identity; (pi/2,0,pi) and (-pi/2,pi,0) ->
+ *    w |-> (-w0, w2, w1); (pi/2,0,0) -> w |-> (w0, w2, -w1));
+ *  - the joint origin xyz in the parent frame (the reference's tz_j1..ty_j7,
+ *    dynamicsGradient.h:223-229). */
+#ifdef FRG_MODEL_TABLES
+#include FRG_MODEL_TABLES
+#else
+#include "../fast-rbd-gradients_gb300/csrc/frg_model_iiwa14.h"
+#endif
+static const double kLinkInertial[7][10] = FRG_MODEL_LINK_INERTIAL;
+static const double kJointFT[7][9] = FRG_MODEL_JOINT_F;
+static const double kJointOrigin[7][3] = FRG_MODEL_JOINT_ORIGIN;
 
 #define REAL double
 #define FN(name) name##_f64

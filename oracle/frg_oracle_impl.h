@@ -255,16 +255,20 @@ static void FN(compute_minv)(REAL *Minv, const REAL *X, const REAL *I) {
  *     df_k = I_k da_k + dv_k x* (I_k v_k) + v_k x* (I_k dv_k)
  *   backward (links k = 6..1): dF_{k-1} += X_k^T dF_k  (+ X_k^T (S x* f_k) for
  *     q at k == c),  dtau_k = dF_k[2];  damping adds 0.5 to d tau_c / d qd_c.
- * Column 0 of d tau / d q is identically zero for this model (the base joint is
- * parallel to gravity), as the reference sets it (:797-813). */
+ * Column 0 of d tau / d q is identically zero when the base joint is parallel
+ * to gravity (the iiwa; the reference sets it so, :797-813): it is skipped
+ * then, and computed from the base's zero velocity and gravity otherwise. */
 static void FN(dtau_columns)(REAL *cdq, REAL *cdqd, const REAL *v, const REAL *a, const REAL *f, const REAL *X,
-                             const REAL *I, const REAL *qd, int damping) {
+                             const REAL *I, const REAL *qd, int damping, int mpc) {
+    /* X_0 v_base = 0 and X_0 a_base (gravity as base acceleration) for column 0 */
+    REAL v_base[6] = {0, 0, 0, 0, 0, 0}, a_base[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 3; i < 6; i++) a_base[i] = mpc ? (REAL)0 : X[i + 6 * 5] * (REAL)kGravity;
     for (int side = 0; side < 2; side++) {
         REAL *out = side == 0 ? cdq : cdqd;
         for (int c = 0; c < NJ; c++) {
             REAL dF[NJ * 6];
             for (int i = 0; i < NJ * 6; i++) dF[i] = 0;
-            if (!(side == 0 && c == 0)) {
+            if (!(side == 0 && c == 0 && FRG_MODEL_DQ_COLUMN0_ZERO)) {
                 REAL dv[6], da[6];
                 for (int k = c; k < NJ; k++) {
                     const REAL *Xk = &X[36 * k], *Ik = &I[36 * k], *vk = &v[6 * k];
@@ -272,7 +276,8 @@ static void FN(dtau_columns)(REAL *cdq, REAL *cdqd, const REAL *v, const REAL *a
                     if (k == c) {
                         if (side == 0) {
                             REAL Xv[6];
-                            FN(xform_motion)(Xv, Xk, &v[6 * (k - 1)], 0);
+                            if (k > 0) FN(xform_motion)(Xv, Xk, &v[6 * (k - 1)], 0);
+                            else for (int i = 0; i < 6; i++) Xv[i] = v_base[i];
                             FN(cross_motion_S)(ndv, Xv, 1, 0);
                         } else {
                             for (int i = 0; i < 6; i++) ndv[i] = 0;
@@ -285,7 +290,8 @@ static void FN(dtau_columns)(REAL *cdq, REAL *cdqd, const REAL *v, const REAL *a
                     if (k == c) {
                         if (side == 0) {
                             REAL Xa[6];
-                            FN(xform_motion)(Xa, Xk, &a[6 * (k - 1)], 0);
+                            if (k > 0) FN(xform_motion)(Xa, Xk, &a[6 * (k - 1)], 0);
+                            else for (int i = 0; i < 6; i++) Xa[i] = a_base[i];
                             FN(cross_motion_S)(nda, Xa, 1, 1);
                         } else {
                             FN(cross_motion_S)(nda, vk, 1, 1);
@@ -346,7 +352,7 @@ static void FN(knot_gradient)(const REAL *q, const REAL *qd, const REAL *u, cons
     FN(rnea_forward)(v, a, f, X, I, qd, qdd, fext, mpc);
     FN(rnea_backward)(NULL, f, X);
     REAL cdu[2 * NJ * NJ];
-    FN(dtau_columns)(cdu, &cdu[NJ * NJ], v, a, f, X, I, qd, damping);
+    FN(dtau_columns)(cdu, &cdu[NJ * NJ], v, a, f, X, I, qd, damping, mpc);
     /* dqdd = -Minv_sym * cdu (matMultSym, math.h:17-25, call :933) */
     for (int col = 0; col < 2 * NJ; col++)
         for (int r = 0; r < NJ; r++) {
@@ -371,7 +377,7 @@ static void FN(knot_gradient_given)(const REAL *q, const REAL *qd, const REAL *q
     FN(rnea_forward)(v, a, f, X, I, qd, qdd, NULL, mpc);
     FN(rnea_backward)(NULL, f, X);
     REAL cdu[2 * NJ * NJ];
-    FN(dtau_columns)(cdu, &cdu[NJ * NJ], v, a, f, X, I, qd, damping);
+    FN(dtau_columns)(cdu, &cdu[NJ * NJ], v, a, f, X, I, qd, damping, mpc);
     for (int col = 0; col < 2 * NJ; col++)
         for (int r = 0; r < NJ; r++) {
             REAL acc = 0;
