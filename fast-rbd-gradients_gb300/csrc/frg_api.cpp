@@ -336,6 +336,20 @@ frg_status frg_discrete_jacobians(frg_ctx *ctx, int n_knots, const float *dqdd, 
     return FRG_OK;
 }
 
+frg_status frg_gradient_knots(frg_ctx *ctx, int n_knots, float *knots, float *dqdd, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_knots < 0 || (n_knots > 0 && !(knots && dqdd))) {
+        frg_set_error(ctx, "frg_gradient_knots: negative n_knots or null pointer");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n_knots == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    if (!check(ctx, frg::launch_knots(ctx->damping, ctx->mpc, ctx->shape, n_knots, knots, dqdd, stream),
+               "frg_gradient_knots launch"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
 frg_status frg_knot_status(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
                            const float *dqdd, const float *qdd, const float *minv, uint32_t *status,
                            frg_stream stream) {

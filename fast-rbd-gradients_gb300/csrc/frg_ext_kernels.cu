@@ -6,6 +6,9 @@
 //       x = [q; qd],  x+ = x + dt [qd; q̈(q, qd, u)]
 //       A = dx+/dx = I + dt [0 I; dq̈/dq dq̈/dqd]   (14 x 14, column-major)
 //       B = dx+/du = dt [0; Minv]                 (14 x 7, column-major)
+//   - the gradient over the reference's packed knot records (knot<T>,
+//     helpers_CPU/dynamicsGradient.h:19-25): [q | qd | u | qdd | Minv], 77
+//     floats per knot, q̈ and Minv written back into the records.
 #include "frg_kernels.cuh"
 #include "frg_knot.cuh"
 
@@ -29,6 +32,28 @@ __global__ void __launch_bounds__(8 * 32)
                           minv ? minv + 49 * g : nullptr, FEXT ? fext + 42 * g : nullptr};
         }
         process_tile<DAMP, MPC, false, FEXT, FDONLY>(ws, lane, kp);
+    }
+}
+
+// Knot records [n][77]: q, qd, u read from each record, q̈ and Minv written
+// into its qdd and Minv fields, the gradient to dqdd [n][98].  The records are
+// not tile-contiguous per array, so gather and scatter resolve every knot's
+// address; inputs are staged before any output is written, and the fields do
+// not overlap.
+template <bool DAMP, bool MPC>
+__global__ void __launch_bounds__(8 * 32) grad_knots_kernel(float *knots, float *dqdd, int n) {
+    extern __shared__ float4 smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    const int wpc = blockDim.x >> 5, ntiles = (n + 31) / 32;
+    for (int tile = blockIdx.x * wpc + warp; tile < ntiles; tile += gridDim.x * wpc) {
+        const long long g = static_cast<long long>(tile) * 32 + lane;
+        KnotPtrs kp{};
+        if (g < n) {
+            float *rec = knots + kKnotRecordFloats * g;
+            kp = KnotPtrs{rec, rec + 7, rec + 14, dqdd + 98 * g, rec + 21, rec + 28};
+        }
+        process_tile<DAMP, MPC>(ws, lane, kp);
     }
 }
 
@@ -102,6 +127,9 @@ cudaError_t dispatch(bool d, bool m, const LaunchShape &sh, int n, const float *
 
 cudaError_t init_ext_kernels() {
     cudaError_t e = cudaSuccess;
+    for (cudaError_t r : {opt_in(grad_knots_kernel<false, false>), opt_in(grad_knots_kernel<true, false>),
+                          opt_in(grad_knots_kernel<false, true>), opt_in(grad_knots_kernel<true, true>)})
+        if (r != cudaSuccess && e == cudaSuccess) e = r;
 #define FRG_OPT(F, O)                                                                                        \
     for (cudaError_t r : {opt_in(grad_ext_kernel<false, false, F, O>), opt_in(grad_ext_kernel<true, false, F, O>), \
                           opt_in(grad_ext_kernel<false, true, F, O>), opt_in(grad_ext_kernel<true, true, F, O>)})  \
@@ -133,6 +161,19 @@ cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     discretize_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(n, dqdd, minv, dt, A, B);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_knots(bool damping, bool mpc, const LaunchShape &shape, int n, float *knots, float *dqdd,
+                         cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    if (shape.warps_per_cta < 1 || shape.warps_per_cta > 8) return cudaErrorInvalidValue;
+    const int w = shape.warps_per_cta, ntiles = (n + 31) / 32, grid = (ntiles + w - 1) / w;
+    const size_t smem = sizeof(WarpSmem) * w;
+    if (!damping && !mpc) grad_knots_kernel<false, false><<<grid, w * 32, smem, stream>>>(knots, dqdd, n);
+    else if (damping && !mpc) grad_knots_kernel<true, false><<<grid, w * 32, smem, stream>>>(knots, dqdd, n);
+    else if (!damping && mpc) grad_knots_kernel<false, true><<<grid, w * 32, smem, stream>>>(knots, dqdd, n);
+    else grad_knots_kernel<true, true><<<grid, w * 32, smem, stream>>>(knots, dqdd, n);
     return cudaGetLastError();
 }
 

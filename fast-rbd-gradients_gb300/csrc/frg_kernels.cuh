@@ -87,6 +87,11 @@ cudaError_t launch_ext(bool damping, bool mpc, const LaunchShape &shape, int n, 
                        cudaStream_t stream);
 cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float dt, float *A, float *B,
                               cudaStream_t stream);
+// The reference's packed knot records [n][kKnotRecordFloats]: q, qd, u in;
+// q̈ and Minv written into the records; the gradient to dqdd [n][98].
+constexpr int kKnotRecordFloats = 77;
+cudaError_t launch_knots(bool damping, bool mpc, const LaunchShape &shape, int n, float *knots, float *dqdd,
+                         cudaStream_t stream);
 // Per-knot non-finite flags (bit 0 inputs, bit 1 outputs; NULL arrays skipped).
 cudaError_t launch_knot_status(int num_sms, int n, const float *q, const float *qd, const float *u,
                                const float *dqdd, const float *qdd, const float *minv, unsigned int *status,

@@ -35,7 +35,7 @@ EXPORTED = (
     "frg_server_create", "frg_server_destroy", "frg_server_submit", "frg_server_poll", "frg_server_wait",
     "frg_server_wait_any", "frg_server_release", "frg_server_get_stats", "frg_gradient_fext",
     "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64", "frg_get_tuning",
-    "frg_set_tuning", "frg_knot_status", "frg_model_name",
+    "frg_set_tuning", "frg_knot_status", "frg_model_name", "frg_gradient_knots",
 )
 
 KNOT_NONFINITE_INPUT = 1
@@ -137,6 +137,7 @@ def _declare(L):
         "frg_set_tuning": (st, [vp, ctypes.POINTER(Tuning)]),
         "frg_knot_status": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
         "frg_model_name": (ctypes.c_char_p, []),
+        "frg_gradient_knots": (st, [vp, i32, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -311,6 +312,12 @@ class Context:
         """Explicit-Euler A [n][14x14], B [n][14x7] from dqdd and minv (device buffers)."""
         self._check(lib().frg_discrete_jacobians(self._h, int(n_knots), _ptr(dqdd), _ptr(minv), float(dt), _ptr(A),
                                                  _ptr(B), _stream_ptr(stream)), "frg_discrete_jacobians")
+
+    def gradient_knots(self, n_knots, knots, dqdd, stream=None):
+        """The reference's packed knot records [n, 77] (device): q, qd, u in;
+        q̈ and Minv written into the records; the gradient to dqdd [n, 98]."""
+        self._check(lib().frg_gradient_knots(self._h, int(n_knots), _ptr(knots), _ptr(dqdd), _stream_ptr(stream)),
+                    "frg_gradient_knots")
 
     def knot_status(self, n_knots, q, qd, u, dqdd, qdd, minv, status, stream=None):
         """status [n] (uint32/int32 device buffer): KNOT_NONFINITE_INPUT / _OUTPUT flags per knot."""

@@ -121,6 +121,20 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
                              float *dqdd, float *qdd, float *minv);
 
 /*
+ * The reference's own per-knot layout, for callers that already pack it: the
+ * knot<T> record of helpers_CPU/dynamicsGradient.h:19-25, [q 7 | qd 7 | u 7 |
+ * qdd 7 | Minv 49] = FRG_KNOT_RECORD_FLOATS floats per knot, as time_GPU.cu:
+ * 137-158 packs it for dynamicsGradientKernel.  knots [n] (DEVICE) supply q,
+ * qd, u; q̈ and dense Minv are written into each record's qdd and Minv fields
+ * (the reference fills them on the host first, forwardDynamics at
+ * time_GPU.cu:134); the gradient goes to dqdd [n][98].  Asynchronous on
+ * `stream`; the same arithmetic and bits as frg_gradient, one knot per lane
+ * whatever the lanes-per-knot setting.
+ */
+#define FRG_KNOT_RECORD_FLOATS 77
+frg_status frg_gradient_knots(frg_ctx *ctx, int n_knots, float *knots, float *dqdd, frg_stream stream);
+
+/*
  * Either side of the gradient (plain path, DEVICE arrays, asynchronous):
  *  - frg_gradient_fext: the gradient with external spatial forces on the links,
  *    fext [n][7][6] (link k's force in its own frame, [n, f] order), subtracted

@@ -78,3 +78,31 @@ def test_discrete_jacobians():
     Bgot = B.cpu().numpy().reshape(n, 7, 14).transpose(0, 2, 1)
     assert max_err(Agot.reshape(n, -1), Aref.reshape(n, -1)) <= TOL
     assert max_err(Bgot.reshape(n, -1), Bref.reshape(n, -1)) <= TOL
+
+
+@pytest.mark.parametrize("damping,mpc", [(0, 0), (1, 1)])
+@pytest.mark.parametrize("n", [1, 33, 1000])
+def test_gradient_over_reference_knot_records(damping, mpc, n):
+    """frg_gradient_knots on the reference's packed records [q|qd|u|qdd|Minv]
+    (77 floats per knot): q̈ and Minv land in the records' fields and, with the
+    gradient, carry the same bits as frg_gradient on separate arrays; q, qd, u
+    are left as they were."""
+    import torch
+    q, qd, u = frg.sample_knots(n, seed=600 + n)
+    rec = np.full((n, 77), np.nan, np.float32)
+    rec[:, 0:7], rec[:, 7:14], rec[:, 14:21] = q, qd, u
+    trec = torch.from_numpy(rec).cuda()
+    tq, tqd, tu = dev(torch, q, qd, u)
+    d_rec = torch.empty((n, 98), device="cuda")
+    ref = [torch.empty((n, w), device="cuda") for w in (98, 7, 49)]
+    with frg.Context(vel_damping=damping, mpc_mode=mpc) as ctx:
+        ctx.gradient_knots(n, trec, d_rec)
+        ctx.gradient(n, tq, tqd, tu, *ref)
+        torch.cuda.synchronize()
+    got = trec.cpu().numpy()
+    assert np.array_equal(got[:, :21], rec[:, :21])
+    assert np.array_equal(d_rec.cpu().numpy(), ref[0].cpu().numpy())
+    assert np.array_equal(got[:, 21:28], ref[1].cpu().numpy())
+    assert np.array_equal(got[:, 28:77], ref[2].cpu().numpy())
+    rd, rq, rm = frg_oracle.gradient_f64(q, qd, u, damping, mpc)
+    assert max_err(d_rec.cpu().numpy(), rd) <= TOL and max_err(got[:, 28:77], rm) <= TOL
