@@ -188,3 +188,22 @@ def test_thread_mappings_give_identical_bits(damping, mpc):
     for name, x, y in zip(("dqdd", "qdd", "minv"), a, b):
         diff = np.count_nonzero(x != y)
         assert diff == 0, f"{name}: {diff} values differ, max {max_err(x, y):.2e}"
+
+
+@pytest.mark.parametrize("lanes", [1, 8])
+def test_angles_beyond_pi_and_large_inputs(lanes):
+    """Joint angles outside [-pi, pi] (up to +-60 rad: the range-reducing sincos
+    path of the FP32 kernels), and velocities and torques ten times the
+    experiment ranges, against the FP64 oracle on the same FP32 inputs."""
+    n = 2048
+    q, qd, u = frg.sample_knots(n, seed=314)
+    rng = np.random.default_rng(15)
+    q = (q + rng.choice([-60.0, -7.0, -3.5, 3.5, 7.0, 60.0], size=q.shape)).astype(np.float32)
+    qd = (qd * 10).astype(np.float32)
+    u = (u * 10).astype(np.float32)
+    with frg.Context() as ctx:
+        ctx.set_lanes_per_knot(lanes)
+        d, qq, m = ctx.gradient_host(q, qd, u)
+    rd, rq, rm = frg_oracle.gradient_f64(q, qd, u)
+    assert max_err(d, rd) <= TOL and max_err(qq, rq) <= TOL and max_err(m, rm) <= TOL
+    assert np.isfinite(d).all()
