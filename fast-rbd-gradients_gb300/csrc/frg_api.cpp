@@ -171,6 +171,7 @@ const char *frg_status_string(frg_status s) {
         case FRG_ERR_SHUTDOWN: return "shut down";
         case FRG_ERR_NOT_FOUND: return "not found";
         case FRG_ERR_INTERNAL: return "internal error";
+        case FRG_ERR_CANCELLED: return "cancelled";
     }
     return "unknown status";
 }

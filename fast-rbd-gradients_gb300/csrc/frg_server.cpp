@@ -580,6 +580,35 @@ frg_status frg_server_release(frg_server *s, uint64_t traj_id) {
     return FRG_OK;
 }
 
+frg_status frg_server_cancel(frg_server *s, uint64_t request_id) {
+    if (!s) return FRG_ERR_INVALID_ARGUMENT;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->reqs.find(request_id);
+        if (it == s->reqs.end() || it->second->consumed) return FRG_ERR_NOT_FOUND;
+        Request *r = it->second.get();
+        if (r->state != ReqState::Admission && r->state != ReqState::Ready) {
+            frg_set_error(s->ctx, "frg_server_cancel: the call is already on the GPU or done");
+            return FRG_ERR_NOT_READY;
+        }
+        std::deque<Request *> &q = r->state == ReqState::Admission ? s->admission : s->ready;
+        q.erase(std::find(q.begin(), q.end(), r));
+        r->staged.clear();
+        r->staged.shrink_to_fit();
+        r->state = ReqState::Done;  // completed, without results: waiters wake and see the status
+        r->status = FRG_ERR_CANCELLED;
+        r->t_launch = r->t_done = Clock::now();
+        auto t = s->trajs.find(r->traj);
+        if (t != s->trajs.end()) t->second.busy = false;
+        s->completions.push_back(r->id);
+        s->st.cancelled++;
+    }
+    s->cv_done.notify_all();
+    s->kick.store(true, std::memory_order_release);
+    s->cv_dispatch.notify_one();  // the head of the admission queue may have changed
+    return FRG_OK;
+}
+
 frg_status frg_server_get_stats(frg_server *s, frg_server_stats *out) {
     if (!s || !out) return FRG_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(s->mu);

@@ -22,7 +22,7 @@ FRG_OK = 0
 STATUS_NAMES = {
     0: "FRG_OK", 1: "FRG_ERR_INVALID_ARGUMENT", 2: "FRG_ERR_CUDA", 3: "FRG_ERR_OUT_OF_MEMORY",
     4: "FRG_ERR_NOT_READY", 5: "FRG_ERR_ADMISSION", 6: "FRG_ERR_TIMEOUT", 7: "FRG_ERR_SHUTDOWN",
-    8: "FRG_ERR_NOT_FOUND", 9: "FRG_ERR_INTERNAL",
+    8: "FRG_ERR_NOT_FOUND", 9: "FRG_ERR_INTERNAL", 10: "FRG_ERR_CANCELLED",
 }
 
 # every symbol include/frg.h declares (checked by tests/test_abi.py)
@@ -35,7 +35,7 @@ EXPORTED = (
     "frg_server_create", "frg_server_destroy", "frg_server_submit", "frg_server_poll", "frg_server_wait",
     "frg_server_wait_any", "frg_server_release", "frg_server_get_stats", "frg_gradient_fext",
     "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64", "frg_get_tuning",
-    "frg_set_tuning", "frg_knot_status", "frg_model_name", "frg_gradient_knots",
+    "frg_set_tuning", "frg_knot_status", "frg_model_name", "frg_gradient_knots", "frg_server_cancel",
 )
 
 KNOT_NONFINITE_INPUT = 1
@@ -87,7 +87,7 @@ class ServerStats(ctypes.Structure):
                 ("knots", ctypes.c_uint64), ("admission_stalls", ctypes.c_uint64), ("rejected", ctypes.c_uint64),
                 ("pool_bytes_cap", ctypes.c_size_t), ("pool_bytes_used", ctypes.c_size_t),
                 ("pool_bytes_peak", ctypes.c_size_t), ("queued_admission", ctypes.c_size_t),
-                ("queued_ready", ctypes.c_size_t)]
+                ("queued_ready", ctypes.c_size_t), ("cancelled", ctypes.c_uint64)]
 
 
 _lib = None
@@ -127,6 +127,7 @@ def _declare(L):
         "frg_server_wait": (st, [vp, ctypes.c_uint64, i64, ctypes.POINTER(RequestInfo)]),
         "frg_server_wait_any": (st, [vp, i64, ctypes.POINTER(RequestInfo)]),
         "frg_server_release": (st, [vp, ctypes.c_uint64]),
+        "frg_server_cancel": (st, [vp, ctypes.c_uint64]),
         "frg_server_get_stats": (st, [vp, ctypes.POINTER(ServerStats)]),
         "frg_gradient_fext": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
         "frg_forward_dynamics": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp]),
@@ -434,6 +435,10 @@ class Server:
 
     def release(self, traj_id):
         return lib().frg_server_release(self._h, int(traj_id))
+
+    def cancel(self, request_id):
+        """Withdraw a call not yet on the GPU; returns the status code."""
+        return lib().frg_server_cancel(self._h, int(request_id))
 
     def stats(self):
         s = ServerStats()

@@ -53,7 +53,8 @@ typedef enum frg_status {
     FRG_ERR_TIMEOUT = 6,
     FRG_ERR_SHUTDOWN = 7,
     FRG_ERR_NOT_FOUND = 8,
-    FRG_ERR_INTERNAL = 9
+    FRG_ERR_INTERNAL = 9,
+    FRG_ERR_CANCELLED = 10 /* a served call withdrawn by frg_server_cancel */
 } frg_status;
 
 /* Same type as cudaStream_t; NULL is the legacy default stream. */
@@ -329,6 +330,7 @@ typedef struct frg_server_stats {
     uint64_t rejected;         /* calls that can never fit */
     size_t pool_bytes_cap, pool_bytes_used, pool_bytes_peak;
     size_t queued_admission, queued_ready;
+    uint64_t cancelled;        /* calls withdrawn by frg_server_cancel */
 } frg_server_stats;
 
 void frg_server_options_default(frg_server_options *opt);
@@ -350,6 +352,14 @@ frg_status frg_server_wait(frg_server *srv, uint64_t request_id, int64_t timeout
 frg_status frg_server_wait_any(frg_server *srv, int64_t timeout_us, frg_request_info *info);
 /* Frees the trajectory's slots (FRG_ERR_NOT_READY while a call is in flight). */
 frg_status frg_server_release(frg_server *srv, uint64_t traj_id);
+/* Withdraws a call that has not reached the GPU (still waiting for admission
+ * or for the next launch): it completes at once with status
+ * FRG_ERR_CANCELLED and no results (wait / poll / wait_any return it like any
+ * completed call), and its trajectory may be submitted again.
+ * FRG_ERR_NOT_READY if the call is already on the GPU or done,
+ * FRG_ERR_NOT_FOUND if it is unknown or already taken.  No counterpart in the
+ * reference, which has no request queue. */
+frg_status frg_server_cancel(frg_server *srv, uint64_t request_id);
 frg_status frg_server_get_stats(frg_server *srv, frg_server_stats *out);
 
 /* Pinned host memory for the _host calls and the server (NULL on failure). */

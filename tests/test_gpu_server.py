@@ -173,3 +173,37 @@ def test_thread_mapping_threshold_keeps_bits():
     for res in results:
         for a, b in zip(res, plain):
             assert np.array_equal(a, b)
+
+
+def test_cancel_a_call_waiting_for_admission():
+    """A call still waiting for pool space is withdrawn: it completes at once
+    with FRG_ERR_CANCELLED and no results, the calls around it are unaffected,
+    the trajectory can be submitted again, and a call already taken cannot be
+    cancelled."""
+    h = 256
+    q, qd, u = knots(h, 31)
+    with frg.Context() as ctx:
+        plain = ctx.gradient_host(q, qd, u)
+        # room for one 256-knot trajectory (700 B per knot), not two
+        with frg.Server(ctx, pool_bytes=int(700 * h * 1.5)) as srv:
+            st, a = srv.submit(1, q, qd, u)
+            assert st == 0
+            st, b = srv.submit(2, q, qd, u)  # waits until trajectory 1 releases its slot
+            assert st == 0
+            assert srv.cancel(b) == 0
+            st, info = srv.wait(b, timeout_us=5_000_000)
+            assert st == 0 and info.status == 10 and not info.dqdd
+            st, info = srv.wait(a, timeout_us=5_000_000)
+            assert st == 0 and info.status == 0
+            for x, y in zip(frg.Server.results(info), plain):
+                assert np.array_equal(x, y)
+            assert srv.cancel(a) == 8   # taken: not found
+            assert srv.cancel(12345) == 8
+            assert srv.stats()["cancelled"] == 1
+            assert srv.release(1) == 0
+            st, b2 = srv.submit(2, q, qd, u)  # the cancelled trajectory runs normally now
+            assert st == 0
+            st, info = srv.wait(b2, timeout_us=5_000_000)
+            assert st == 0 and info.status == 0
+            for x, y in zip(frg.Server.results(info), plain):
+                assert np.array_equal(x, y)
