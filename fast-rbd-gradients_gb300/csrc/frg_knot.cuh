@@ -79,9 +79,8 @@ __device__ __forceinline__ bool aligned16(const void *p) {
     return (reinterpret_cast<unsigned long long>(p) & 15ull) == 0;
 }
 
-// Coalesced gather of W reals per knot (knot-major) into stage[lane*W + j].
-// Contiguous tiles copy 32*W reals straight (16-byte slots when aligned); other
-// tiles (idle lanes, trajectory boundaries) resolve every knot's base.
+// Gather of W reals per knot (knot-major) into stage[lane*W + j].  Contiguous
+// tiles copy 32*W reals straight and coalesced (16-byte slots when aligned).
 template <int W>
 __device__ __forceinline__ void gather_in(real *stage, const real *base, int lane) {
     const real *b0;
@@ -97,16 +96,16 @@ __device__ __forceinline__ void gather_in(real *stage, const real *base, int lan
         }
         return;
     }
+    // other tiles (idle lanes, knots of several trajectories, strided
+    // records): each lane reads its own knot.  One load per value, no
+    // shuffles or divisions: a partial tile used to cost half a tile more
+    // with the warp-cooperative per-element form, and costs nothing extra now.
 #pragma unroll
-    for (int e = lane; e < 32 * W; e += 32) {
-        const int kn = e / W, j = e - kn * W;
-        const real *p = shfl_ptr(base, kn);
-        stage[e] = p ? __ldg(p + j) : 0.0f;
-    }
+    for (int j = 0; j < W; j++) stage[lane * W + j] = base ? __ldg(base + j) : real(0);
 }
 
-// Coalesced scatter of stage[lane*W + j] to each knot's W reals at base
-// (knots STRIDE reals apart).
+// Scatter of stage[lane*W + j] to each knot's W reals at base (knots STRIDE
+// reals apart): coalesced for contiguous tiles, lane-wise otherwise.
 template <int W, int STRIDE = W>
 __device__ __forceinline__ void scatter_out(const real *stage, real *base, int lane) {
     __syncwarp();
@@ -136,13 +135,9 @@ __device__ __forceinline__ void scatter_out(const real *stage, real *base, int l
                 }
             }
         }
-    } else {
+    } else if (base) {  // other tiles: each lane writes its own knot (see gather_in)
 #pragma unroll 7
-        for (int e = lane; e < 32 * W; e += 32) {
-            const int kn = e / W, j = e - kn * W;
-            real *p = shfl_ptr(base, kn);
-            if (p) p[j] = stage[e];
-        }
+        for (int j = 0; j < W; j++) base[j] = stage[lane * W + j];
     }
     __syncwarp();
 }
