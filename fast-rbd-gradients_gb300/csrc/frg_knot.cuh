@@ -49,6 +49,7 @@ __device__ __forceinline__ double4x ldg4(const double4x *p) {
 struct WarpSmem {
     real4 link[kLinkSlots][32];
     real stage[32 * kStageFloats];
+    const real *knot[32];  // each lane's knot pointer, for tiles that are not one contiguous run
 };
 
 // A lane's knot: input and output bases (q == nullptr: idle lane).
@@ -79,6 +80,18 @@ __device__ __forceinline__ bool aligned16(const void *p) {
     return (reinterpret_cast<unsigned long long>(p) & 15ull) == 0;
 }
 
+// Element e = lane + 32 m (m < W) of a tile's W reals per knot is entry
+// e % W of knot e / W; step (kn, j) from element e to e + 32.
+template <int W>
+__device__ __forceinline__ void next_element(int &kn, int &j) {
+    kn += 32 / W;
+    j += 32 % W;
+    if (j >= W) {
+        j -= W;
+        kn++;
+    }
+}
+
 // Gather of W reals per knot (knot-major) into stage[lane*W + j].  Contiguous
 // tiles copy 32*W reals straight and coalesced (16-byte slots when aligned).
 template <int W>
@@ -96,18 +109,25 @@ __device__ __forceinline__ void gather_in(real *stage, const real *base, int lan
         }
         return;
     }
-    // other tiles (idle lanes, knots of several trajectories, strided
-    // records): each lane reads its own knot.  One load per value, no
-    // shuffles or divisions: a partial tile used to cost half a tile more
-    // with the warp-cooperative per-element form, and costs nothing extra now.
+    // Other tiles (knots of several trajectories, idle lanes, strided
+    // records): each lane reads its own knot, all W loads in flight at once.
 #pragma unroll
     for (int j = 0; j < W; j++) stage[lane * W + j] = base ? __ldg(base + j) : real(0);
 }
 
 // Scatter of stage[lane*W + j] to each knot's W reals at base (knots STRIDE
-// reals apart): coalesced for contiguous tiles, lane-wise otherwise.
+// reals apart in contiguous tiles).  Other tiles (knots of several
+// trajectories, idle lanes, strided records) store element by element through
+// each knot's pointer in the warp's table: consecutive elements of a knot are
+// consecutive in memory, so each store instruction still covers whole runs of
+// a few cache lines.  A lane storing only its own knot would turn every store
+// instruction into 32 separate cache-line writes; with many such tiles in
+// flight the L2 request rate, not the arithmetic, then sets the time.  The
+// stores go in groups of 7 after the group's table and stage reads: the
+// compiler cannot tell a table pointer from shared memory, so a read placed
+// after a store would wait for it.
 template <int W, int STRIDE = W>
-__device__ __forceinline__ void scatter_out(const real *stage, real *base, int lane) {
+__device__ __forceinline__ void scatter_out(const real *stage, real *base, int lane, const real **knot) {
     __syncwarp();
     real *b0;
     if (tile_contiguous<STRIDE>(base, lane, b0)) {
@@ -122,24 +142,35 @@ __device__ __forceinline__ void scatter_out(const real *stage, real *base, int l
                 for (int e = lane; e < 32 * W; e += 32) b0[e] = stage[e];
             }
         } else {
-            // element e = lane + 32 m is knot e / W, entry e % W
-            int kn = lane / W, j = lane - (lane / W) * W;
+            int kn = lane / W, j = lane % W;
 #pragma unroll 7
             for (int e = lane; e < 32 * W; e += 32) {
                 b0[kn * STRIDE + j] = stage[e];
-                kn += 32 / W;
-                j += 32 % W;
-                if (j >= W) {
-                    j -= W;
-                    kn++;
-                }
+                next_element<W>(kn, j);
             }
         }
-    } else if (base) {  // other tiles: each lane writes its own knot (see gather_in)
-#pragma unroll 7
-        for (int j = 0; j < W; j++) base[j] = stage[lane * W + j];
+    } else {
+        static_assert(W % 7 == 0, "split-tile stores go in groups of 7");
+        knot[lane] = base;
+        __syncwarp();
+        int kn = lane / W, j = lane % W;
+#pragma unroll 1
+        for (int m0 = 0; m0 < W; m0 += 7) {
+            real *p[7];
+            real v[7];
+#pragma unroll
+            for (int i = 0; i < 7; i++) {
+                p[i] = const_cast<real *>(knot[kn]);
+                if (p[i]) p[i] += j;
+                v[i] = stage[lane + 32 * (m0 + i)];
+                next_element<W>(kn, j);
+            }
+#pragma unroll
+            for (int i = 0; i < 7; i++)
+                if (p[i]) *p[i] = v[i];
+        }
     }
-    __syncwarp();
+    __syncwarp();  // also: the table is rewritten by the next scatter
 }
 
 __device__ __forceinline__ void lds_link(const WarpSmem *ws, int k, int lane, real v[6], real Iv[6]) {
@@ -645,9 +676,9 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     }
     __syncwarp();
     if constexpr (MIRROR) {
-        scatter_out<7>(ws->stage, const_cast<real *>(mr.q), lane);
-        scatter_out<7>(ws->stage + 224, const_cast<real *>(mr.qd), lane);
-        scatter_out<7>(ws->stage + 448, const_cast<real *>(mr.u), lane);
+        scatter_out<7>(ws->stage, const_cast<real *>(mr.q), lane, ws->knot);
+        scatter_out<7>(ws->stage + 224, const_cast<real *>(mr.qd), lane, ws->knot);
+        scatter_out<7>(ws->stage + 448, const_cast<real *>(mr.u), lane, ws->knot);
     }
     const real *fx = nullptr;
     if constexpr (FEXT) {  // the lane's 42 external-force values stay staged through both RNEA passes
@@ -668,12 +699,12 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     for (int c = 0; c < 7; c++)
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r + 7 * c] = r <= c ? Mi[r][c] : Mi[c][r];
-    scatter_out<49>(ws->stage, kp.minv, lane);
-    if constexpr (MIRROR) scatter_out<49>(ws->stage, mr.minv, lane);
+    scatter_out<49>(ws->stage, kp.minv, lane, ws->knot);
+    if constexpr (MIRROR) scatter_out<49>(ws->stage, mr.minv, lane, ws->knot);
 #pragma unroll
     for (int r = 0; r < 7; r++) ws->stage[lane * 7 + r] = qdd[r];
-    scatter_out<7>(ws->stage, kp.qdd, lane);
-    if constexpr (MIRROR) scatter_out<7>(ws->stage, mr.qdd, lane);
+    scatter_out<7>(ws->stage, kp.qdd, lane, ws->knot);
+    if constexpr (MIRROR) scatter_out<7>(ws->stage, mr.qdd, lane, ws->knot);
     if constexpr (FDONLY) return;
     if constexpr (!FEXT) {
         rnea_with_qdd<MPC>(ws, lane, qd, qdd, sq, cq);
@@ -695,8 +726,8 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
     }
-    scatter_out<49, 98>(ws->stage, kp.dqdd, lane);
-    if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd, lane);
+    scatter_out<49, 98>(ws->stage, kp.dqdd, lane, ws->knot);
+    if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd, lane, ws->knot);
     // d qdd / dqd: columns 7..13
 #pragma unroll 1
     for (int c = 0; c < kJoints; c++) {
@@ -706,8 +737,8 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
     }
-    scatter_out<49, 98>(ws->stage, kp.dqdd ? kp.dqdd + 49 : nullptr, lane);
-    if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd ? mr.dqdd + 49 : nullptr, lane);
+    scatter_out<49, 98>(ws->stage, kp.dqdd ? kp.dqdd + 49 : nullptr, lane, ws->knot);
+    if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd ? mr.dqdd + 49 : nullptr, lane, ws->knot);
 }
 
 }  // namespace FRG_NS
