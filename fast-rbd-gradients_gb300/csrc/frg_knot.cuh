@@ -67,13 +67,16 @@ __device__ __forceinline__ real *shfl_ptr(real *p, int src) {
     return reinterpret_cast<real *>(__shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), src));
 }
 
-// True when lane i's base is lane 0's base + i * STRIDE for all 32 lanes (a
-// tile of 32 consecutive knots of one array); b0 = lane 0's base.  Warp-uniform.
+// The tile's knot count n when its knots are one run in memory: lanes 0..n-1
+// hold knots, lane i's base = lane 0's base + i * STRIDE, and the other lanes
+// are idle (null).  Otherwise 0.  b0 = lane 0's base.  Warp-uniform.
 template <int STRIDE, typename P>
-__device__ __forceinline__ bool tile_contiguous(P base, int lane, P &b0) {
+__device__ __forceinline__ int tile_run(P base, int lane, P &b0) {
     b0 = shfl_ptr(base, 0);
-    const bool mine = base != nullptr && b0 != nullptr && base == b0 + lane * STRIDE;
-    return __all_sync(0xffffffffu, mine);
+    const unsigned valid = __ballot_sync(0xffffffffu, base != nullptr);
+    const bool mine = base == nullptr || (b0 != nullptr && base == b0 + lane * STRIDE);
+    if (!__all_sync(0xffffffffu, mine) || (valid & (valid + 1u)) != 0u) return 0;  // valid lanes: a prefix
+    return __popc(valid);
 }
 
 __device__ __forceinline__ bool aligned16(const void *p) {
@@ -92,21 +95,24 @@ __device__ __forceinline__ void next_element(int &kn, int &j) {
     }
 }
 
-// Gather of W reals per knot (knot-major) into stage[lane*W + j].  Contiguous
-// tiles copy 32*W reals straight and coalesced (16-byte slots when aligned).
+// Gather of W reals per knot (knot-major) into stage[lane*W + j].  Tiles of
+// one run copy their n*W reals straight and coalesced (16-byte slots when the
+// run is 32 knots and aligned); idle lanes get zeros.
 template <int W>
 __device__ __forceinline__ void gather_in(real *stage, const real *base, int lane) {
     const real *b0;
-    if (tile_contiguous<W>(base, lane, b0)) {
-        if (aligned16(b0)) {
-            const real4 *src = reinterpret_cast<const real4 *>(b0);
-            real4 *dst = reinterpret_cast<real4 *>(stage);
+    const int n = tile_run<W>(base, lane, b0);
+    if (n == 32 && aligned16(b0)) {
+        const real4 *src = reinterpret_cast<const real4 *>(b0);
+        real4 *dst = reinterpret_cast<real4 *>(stage);
 #pragma unroll
-            for (int e = lane; e < 8 * W; e += 32) dst[e] = ldg4(src + e);
-        } else {
+        for (int e = lane; e < 8 * W; e += 32) dst[e] = ldg4(src + e);
+        return;
+    }
+    if (n > 0) {
+        const int lim = n * W;
 #pragma unroll
-            for (int e = lane; e < 32 * W; e += 32) stage[e] = __ldg(b0 + e);
-        }
+        for (int e = lane; e < 32 * W; e += 32) stage[e] = e < lim ? __ldg(b0 + e) : real(0);
         return;
     }
     // Other tiles (knots of several trajectories, idle lanes, strided
@@ -116,8 +122,8 @@ __device__ __forceinline__ void gather_in(real *stage, const real *base, int lan
 }
 
 // Scatter of stage[lane*W + j] to each knot's W reals at base (knots STRIDE
-// reals apart in contiguous tiles).  Other tiles (knots of several
-// trajectories, idle lanes, strided records) store element by element through
+// reals apart in tiles of one run).  Other tiles (knots of several
+// trajectories, strided records) store element by element through
 // each knot's pointer in the warp's table: consecutive elements of a knot are
 // consecutive in memory, so each store instruction still covers whole runs of
 // a few cache lines.  A lane storing only its own knot would turn every store
@@ -130,22 +136,25 @@ template <int W, int STRIDE = W>
 __device__ __forceinline__ void scatter_out(const real *stage, real *base, int lane, const real **knot) {
     __syncwarp();
     real *b0;
-    if (tile_contiguous<STRIDE>(base, lane, b0)) {
+    const int n = tile_run<STRIDE>(base, lane, b0);
+    if (n > 0) {
         if constexpr (STRIDE == W) {
-            if (aligned16(b0)) {
+            if (n == 32 && aligned16(b0)) {
                 const real4 *src = reinterpret_cast<const real4 *>(stage);
                 real4 *dst = reinterpret_cast<real4 *>(b0);
 #pragma unroll
                 for (int e = lane; e < 8 * W; e += 32) dst[e] = src[e];
             } else {
+                const int lim = n * W;
 #pragma unroll 7
-                for (int e = lane; e < 32 * W; e += 32) b0[e] = stage[e];
+                for (int e = lane; e < 32 * W; e += 32)
+                    if (e < lim) b0[e] = stage[e];
             }
         } else {
             int kn = lane / W, j = lane % W;
 #pragma unroll 7
             for (int e = lane; e < 32 * W; e += 32) {
-                b0[kn * STRIDE + j] = stage[e];
+                if (kn < n) b0[kn * STRIDE + j] = stage[e];
                 next_element<W>(kn, j);
             }
         }

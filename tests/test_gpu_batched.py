@@ -80,6 +80,51 @@ def test_scattered_trajectories_alone_and_in_mix():
             assert torch.equal(alone, mix)
 
 
+def test_gaps_between_trajectories_stay_untouched():
+    """Trajectories packed into shared buffers with gaps of 0..40 knots between
+    them (tiles that mix up to many trajectories, and ones with idle lanes):
+    the batched and plan results equal the plain kernel's bit for bit, and no
+    value in a gap changes."""
+    import torch
+    rng = np.random.default_rng(31)
+    hs = np.concatenate([rng.integers(1, 12, 60), rng.integers(1, 90, 90)])
+    gaps = rng.integers(0, 41, hs.size)
+    starts = np.concatenate([[0], np.cumsum(hs + gaps)[:-1]])
+    total = int(starts[-1] + hs[-1] + gaps[-1])
+    n = int(hs.sum())
+    q, qd, u = frg.sample_knots(n, seed=77)
+    packed = [np.full((total, 7), 3.0, np.float32) for _ in range(3)]
+    for t, (s, hh) in enumerate(zip(starts, hs)):
+        a = int(hs[:t].sum())
+        for dst, src in zip(packed, (q, qd, u)):
+            dst[s:s + hh] = src[a:a + hh]
+    tq, tqd, tu = (torch.from_numpy(x).cuda() for x in packed)
+    sentinel = -7.25
+    with frg.Context() as ctx:
+        ref = alloc(torch, n)
+        ctx.gradient(n, *(torch.from_numpy(x).cuda() for x in (q, qd, u)), *ref)
+        for form in ("batched", "plan"):
+            out = [torch.full((total, w), sentinel, device="cuda") for w in (98, 7, 49)]
+            trajs = [(int(hh), tq[s:], tqd[s:], tu[s:], out[0][s:], out[1][s:], out[2][s:])
+                     for s, hh in zip(starts, hs)]
+            if form == "batched":
+                ctx.batched(trajs)
+            else:
+                plan = ctx.plan(trajs)
+                try:
+                    plan.launch()
+                    torch.cuda.synchronize()
+                finally:
+                    plan.close()
+            torch.cuda.synchronize()
+            live = torch.zeros(total, dtype=torch.bool, device="cuda")
+            for s, hh in zip(starts, hs):
+                live[s:s + hh] = True
+            for o, r in zip(out, ref):
+                assert torch.equal(o[live], r), form
+                assert bool((o[~live] == sentinel).all()), form
+
+
 def test_plan_graph_replay_tracks_input_changes():
     import torch
     h, off = frg.ragged_horizons(64, 8, 256, seed=5)
