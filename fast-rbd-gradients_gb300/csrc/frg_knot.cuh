@@ -574,83 +574,126 @@ __device__ __forceinline__ void link_force_tangent(real df[6], const real v[6], 
     crf_acc(df, v, Idv);
 }
 
-// One column of d tau / dq (QSIDE) or d tau / dqd for the differentiated joint c
-// (compute_vafdu :787-829 and compute_cdu :832-857 restricted to column c).
-// The forward sweep is software-pipelined: the block of link k computes the
-// force tangent of link k - 1 together with the velocity / acceleration
-// tangents of link k, two independent dependency chains in one basic block
-// (the link loop is unrolled, the column c is a warp-uniform runtime value).
-template <bool QSIDE, bool DAMP>
-__device__ __forceinline__ void dtau_column(const WarpSmem *ws, int lane, int c, const real qd[7],
-                                            const real sq[7], const real cq[7], real dtau[7]) {
-    real df[kJoints][6];
-    real dv[6], da[6];
+// Seed of the tangent sweep for the differentiated joint k, from link k's
+// velocity v: d tau / dq_k (QSIDE) or d tau / dqd_k.
+template <bool QSIDE>
+__device__ __forceinline__ void seed_column(const WarpSmem *ws, int lane, int k, real qdk, const real v[6],
+                                            real dv[6], real da[6]) {
+    if constexpr (QSIDE) {
+        // dv = crm(X_k v_{k-1}) S; (X_k v_{k-1}) and v_k agree outside entry 2
+        dv[0] = v[1]; dv[1] = -v[0]; dv[2] = 0.0f;
+        dv[3] = v[4]; dv[4] = -v[3]; dv[5] = 0.0f;
+        // da = crm(dv) S qd_k + crm(X_k a_{k-1}) S
+        const real4 xa = ws->link[kSlotsPerLink * k + 3][lane];  // (Xa0, Xa1, Xa3, Xa4)
+        da[0] = fmaR(dv[1], qdk, xa.y);
+        da[1] = fmaR(-dv[0], qdk, -xa.x);
+        da[2] = 0.0f;
+        da[3] = fmaR(dv[4], qdk, xa.w);
+        da[4] = fmaR(-dv[3], qdk, -xa.z);
+        da[5] = 0.0f;
+    } else {
+        // dv = S, da = crm(v_k) S
+        dv[0] = dv[1] = 0.0f; dv[2] = 1.0f; dv[3] = dv[4] = dv[5] = 0.0f;
+        da[0] = v[1]; da[1] = -v[0]; da[2] = 0.0f;
+        da[3] = v[4]; da[4] = -v[3]; da[5] = 0.0f;
+    }
+}
+
+// Velocity / acceleration tangents carried from link k - 1 into link k.
+template <int k>
+__device__ __forceinline__ void advance_column(real dv[6], real da[6], real qdk, real ck, real sk) {
+    real ndv[6], nda[6];
+    xmotion<k>(ndv, dv, ck, sk);
+    xmotion<k>(nda, da, ck, sk);
+    nda[0] = fmaR(ndv[1], qdk, nda[0]);
+    nda[1] = fmaR(-ndv[0], qdk, nda[1]);
+    nda[3] = fmaR(ndv[4], qdk, nda[3]);
+    nda[4] = fmaR(-ndv[3], qdk, nda[4]);
+#pragma unroll
+    for (int i = 0; i < 6; i++) { dv[i] = ndv[i]; da[i] = nda[i]; }
+}
+
+// Columns c and c + 1 of d tau / dq (QSIDE) or d tau / dqd, for the
+// differentiated joints c and c + 1 (compute_vafdu :787-829 and compute_cdu
+// :832-857 restricted to those columns); c + 1 == kJoints or !PAIR computes
+// column c only.  The two columns are independent dependency chains through the same
+// link loads; each does exactly the operations of a single-column sweep, so
+// the bits do not depend on the pairing.  The forward sweep is also
+// software-pipelined: the block of link k computes the force tangents of link
+// k - 1 with the velocity / acceleration tangents of link k.  The link loop is
+// unrolled; c is a warp-uniform runtime value.
+template <bool QSIDE, bool DAMP, bool PAIR>
+__device__ __forceinline__ void dtau_column_pair(const WarpSmem *ws, int lane, int c, const real qd[7],
+                                                 const real sq[7], const real cq[7], real dtA[7], real dtB[7]) {
+    const int cb = PAIR ? c + 1 : kJoints;
+    real dfA[kJoints][6], dfB[kJoints][6];
+    real dvA[6], daA[6], dvB[6], daB[6];
+#pragma unroll
+    for (int i = 0; i < 6; i++) dvB[i] = daB[i] = 0.0f;
     static_for<0, kJoints>([&](auto K) {
         constexpr int k = decltype(K)::value;
         if (k == c) {
             real v[6], Iv[6];
             lds_link(ws, k, lane, v, Iv);
-            if constexpr (QSIDE) {
-                // dv = crm(X_k v_{k-1}) S; (X_k v_{k-1}) and v_k agree outside entry 2
-                dv[0] = v[1]; dv[1] = -v[0]; dv[2] = 0.0f;
-                dv[3] = v[4]; dv[4] = -v[3]; dv[5] = 0.0f;
-                // da = crm(dv) S qd_k + crm(X_k a_{k-1}) S
-                const real4 xa = ws->link[kSlotsPerLink * k + 3][lane];  // (Xa0, Xa1, Xa3, Xa4)
-                da[0] = fmaR(dv[1], qd[k], xa.y);
-                da[1] = fmaR(-dv[0], qd[k], -xa.x);
-                da[2] = 0.0f;
-                da[3] = fmaR(dv[4], qd[k], xa.w);
-                da[4] = fmaR(-dv[3], qd[k], -xa.z);
-                da[5] = 0.0f;
-            } else {
-                // dv = S, da = crm(v_k) S
-                dv[0] = dv[1] = 0.0f; dv[2] = 1.0f; dv[3] = dv[4] = dv[5] = 0.0f;
-                da[0] = v[1]; da[1] = -v[0]; da[2] = 0.0f;
-                da[3] = v[4]; da[4] = -v[3]; da[5] = 0.0f;
-            }
+            seed_column<QSIDE>(ws, lane, k, qd[k], v, dvA, daA);
         } else if (k > c) {
             if constexpr (k >= 1) {
                 real v[6], Iv[6];
                 lds_link(ws, k - 1, lane, v, Iv);
-                link_force_tangent<k - 1>(df[k - 1], v, Iv, dv, da);
-                real ndv[6], nda[6];
-                xmotion<k>(ndv, dv, cq[k], sq[k]);
-                xmotion<k>(nda, da, cq[k], sq[k]);
-                nda[0] = fmaR(ndv[1], qd[k], nda[0]);
-                nda[1] = fmaR(-ndv[0], qd[k], nda[1]);
-                nda[3] = fmaR(ndv[4], qd[k], nda[3]);
-                nda[4] = fmaR(-ndv[3], qd[k], nda[4]);
-#pragma unroll
-                for (int i = 0; i < 6; i++) { dv[i] = ndv[i]; da[i] = nda[i]; }
+                link_force_tangent<k - 1>(dfA[k - 1], v, Iv, dvA, daA);
+                if (k > cb) link_force_tangent<k - 1>(dfB[k - 1], v, Iv, dvB, daB);
+                advance_column<k>(dvA, daA, qd[k], cq[k], sq[k]);
+                if (k > cb) advance_column<k>(dvB, daB, qd[k], cq[k], sq[k]);
+                if (k == cb) {
+                    real vb[6], Ivb[6];
+                    lds_link(ws, k, lane, vb, Ivb);
+                    seed_column<QSIDE>(ws, lane, k, qd[k], vb, dvB, daB);
+                }
             }
         }
     });
     {
         real v[6], Iv[6];
         lds_link(ws, kJoints - 1, lane, v, Iv);
-        link_force_tangent<kJoints - 1>(df[kJoints - 1], v, Iv, dv, da);
+        link_force_tangent<kJoints - 1>(dfA[kJoints - 1], v, Iv, dvA, daA);
+        if (cb < kJoints) link_force_tangent<kJoints - 1>(dfB[kJoints - 1], v, Iv, dvB, daB);
     }
-    real dF[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    real dFA[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, dFB[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     static_for_down<kJoints - 1, 0>([&](auto K) {
         constexpr int k = decltype(K)::value;
         if (k >= c) {
 #pragma unroll
-            for (int i = 0; i < 6; i++) dF[i] += df[k][i];
+            for (int i = 0; i < 6; i++) dFA[i] += dfA[k][i];
         }
-        dtau[k] = dF[2];
+        if (k >= cb) {
+#pragma unroll
+            for (int i = 0; i < 6; i++) dFB[i] += dfB[k][i];
+        }
+        dtA[k] = dFA[2];
+        dtB[k] = dFB[2];
         if constexpr (k > 0) {
-            if (QSIDE && k == c) {
+            if (QSIDE && (k == c || k == cb)) {
                 // + X_k^T (S x* f_k)
                 const real4 fs = ws->link[kSlotsPerLink * k + 4][lane];  // (f0, f1, f3, f4)
+                real *dF = k == c ? dFA : dFB;
                 dF[0] -= fs.y; dF[1] += fs.x; dF[3] -= fs.w; dF[4] += fs.z;
             }
             real t[6];
-            xforce_T<k>(t, dF, cq[k], sq[k]);
+            xforce_T<k>(t, dFA, cq[k], sq[k]);
 #pragma unroll
-            for (int i = 0; i < 6; i++) dF[i] = t[i];
+            for (int i = 0; i < 6; i++) dFA[i] = t[i];
+            xforce_T<k>(t, dFB, cq[k], sq[k]);
+#pragma unroll
+            for (int i = 0; i < 6; i++) dFB[i] = t[i];
         }
     });
-    if (!QSIDE && DAMP) dtau[c] += 0.5f;
+    if constexpr (!QSIDE && DAMP) {  // compile-time indices: no local-memory array
+#pragma unroll
+        for (int k = 0; k < kJoints; k++) {
+            if (k == c) dtA[k] += 0.5f;
+            if (k == cb) dtB[k] += 0.5f;
+        }
+    }
 }
 
 // out = -Minv_sym dtau
@@ -727,24 +770,36 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r] = 0.0f;
     }
+    // two columns per sweep; one with FEXT, whose staged forces leave fewer registers
+    constexpr bool kPair = !FEXT;
 #pragma unroll 1
-    for (int c = kDqColumn0Zero ? 1 : 0; c < kJoints; c++) {
-        real dtau[7], out[7];
-        dtau_column<true, DAMP>(ws, lane, c, qd, sq, cq, dtau);
-        minv_times(out, Mi, dtau);
+    for (int c = kDqColumn0Zero ? 1 : 0; c < kJoints; c += kPair ? 2 : 1) {
+        real dtA[7], dtB[7], out[7];
+        dtau_column_pair<true, DAMP, kPair>(ws, lane, c, qd, sq, cq, dtA, dtB);
+        minv_times(out, Mi, dtA);
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
+        if (kPair && c + 1 < kJoints) {
+            minv_times(out, Mi, dtB);
+#pragma unroll
+            for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * (c + 1) + r] = out[r];
+        }
     }
     scatter_out<49, 98>(ws->stage, kp.dqdd, lane, ws->knot);
     if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd, lane, ws->knot);
     // d qdd / dqd: columns 7..13
 #pragma unroll 1
-    for (int c = 0; c < kJoints; c++) {
-        real dtau[7], out[7];
-        dtau_column<false, DAMP>(ws, lane, c, qd, sq, cq, dtau);
-        minv_times(out, Mi, dtau);
+    for (int c = 0; c < kJoints; c += kPair ? 2 : 1) {
+        real dtA[7], dtB[7], out[7];
+        dtau_column_pair<false, DAMP, kPair>(ws, lane, c, qd, sq, cq, dtA, dtB);
+        minv_times(out, Mi, dtA);
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
+        if (kPair && c + 1 < kJoints) {
+            minv_times(out, Mi, dtB);
+#pragma unroll
+            for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * (c + 1) + r] = out[r];
+        }
     }
     scatter_out<49, 98>(ws->stage, kp.dqdd ? kp.dqdd + 49 : nullptr, lane, ws->knot);
     if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd ? mr.dqdd + 49 : nullptr, lane, ws->knot);
