@@ -79,11 +79,14 @@ bool frg_offsets_to_trajs(int n_traj, const int64_t *offsets, const float *q, co
                           float *dqdd, float *qdd, float *minv, std::vector<frg_traj> &out);
 
 namespace frg {
-// Launch shape used until the autotuner or the caller picks one.
+// Launch shape used until the autotuner or the caller picks one: 2-warp CTAs,
+// 4 per SM.  The knot-per-lane kernels use up to 255 registers, so each
+// quadrant of the register file holds two of their warps (8 per SM); 3-warp
+// CTAs would leave only 2 CTAs, 6 warps, resident.
 inline LaunchShape default_shape() {
     LaunchShape s;
-    s.warps_per_cta = 3;
-    s.ctas_per_sm = 3;
+    s.warps_per_cta = 2;
+    s.ctas_per_sm = 4;
     return s;
 }
 }  // namespace frg

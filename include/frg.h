@@ -71,8 +71,8 @@ typedef struct frg_options {
                           dtau/dqd diagonal (default 0, experiment_helpers.h:20) */
     int mpc_mode;      /* MPC_MODE: gravity-compensated arm, base acceleration 0
                           (default 0, dynamicsGradient.h:635-637) */
-    int warps_per_cta; /* 0 = engine default */
-    int ctas_per_sm;   /* 0 = engine default (persistent batched launches) */
+    int warps_per_cta; /* 0 = engine default (2) */
+    int ctas_per_sm;   /* 0 = engine default (4; persistent batched launches) */
     int lanes_per_knot; /* 0 = default (1); 1 = one knot per lane, 32 knots per
                            warp (throughput); 8 = one knot per 8 lanes, 4 knots
                            per warp (latency: small batches finish ~2.5x sooner) */
