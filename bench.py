@@ -16,6 +16,9 @@ through the full path (RNEA, Minv, q̈, dtau/dq, dtau/dqd, -Minv dtau) in FP32.
             {16, 32, 64, 128, 1024, 65536} (L2 warm), plus N = 1 (single-knot
             latency) and N = 65536 over batches larger than L2; the faster
             thread mapping kept.
+  entry_points  the calls either side of the gradient (external forces,
+            forward dynamics, knot records, discrete Jacobians, the FP64
+            build) on 65,536 knots, L2 flushed: time per launch.
   served    p50/p99 request latency of the continuous-batching server, and
             the 2 GiB-pool admission run with 1 % of its calls verified by
             the FP64 GPU build.
@@ -206,6 +209,63 @@ def plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak, steps=20):
                     "fp32_frac": FLOP_PER_KNOT_REF * n / (ms * 1e-3) / 1e12 / fp32_peak})
     ctx.set_tuning(saved)
     return out
+
+
+def entry_points(ctx, torch, dev, stream, peaks, n=65536, steps=20):
+    """The entry points either side of the gradient, each on n contiguous
+    device-resident knots over FLUSH_SETS rotating batches (larger than L2),
+    with the context's plain launch shape: CUDA-event time per launch and the
+    algorithmic bytes each moves per knot (inputs + outputs)."""
+    import frg
+    f32, f64 = torch.float32, torch.float64
+    sets = []
+    for i in range(FLUSH_SETS):
+        q, qd, u = frg.sample_knots(n, seed=500 + i)
+        t = {k: torch.from_numpy(x).to(dev) for k, x in (("q", q), ("qd", qd), ("u", u))}
+        t["fext"] = torch.randn((n, 42), device=dev, dtype=f32)
+        for k, w in (("dqdd", 98), ("qdd", 7), ("minv", 49), ("A", 196), ("B", 98)):
+            t[k] = torch.empty((n, w), device=dev, dtype=f32)
+        t["knots"] = torch.zeros((n, 77), device=dev, dtype=f32)
+        t["knots"][:, 0:7], t["knots"][:, 7:14], t["knots"][:, 14:21] = t["q"], t["qd"], t["u"]
+        for k in ("q", "qd", "u"):
+            t[k + "64"] = t[k].to(f64)
+        for k, w in (("dqdd64", 98), ("qdd64", 7), ("minv64", 49)):
+            t[k] = torch.empty((n, w), device=dev, dtype=f64)
+        sets.append(t)
+    calls = {
+        "gradient": (700, lambda t: ctx.gradient(n, t["q"], t["qd"], t["u"], t["dqdd"], t["qdd"], t["minv"],
+                                                 stream=stream)),
+        "gradient_fext": (868, lambda t: ctx.gradient_fext(n, t["q"], t["qd"], t["u"], t["fext"], t["dqdd"],
+                                                           t["qdd"], t["minv"], stream=stream)),
+        "forward_dynamics (qdd)": (112, lambda t: ctx.forward_dynamics(n, t["q"], t["qd"], t["u"], t["qdd"],
+                                                                      stream=stream)),
+        "forward_dynamics (qdd, Minv)": (308, lambda t: ctx.forward_dynamics(n, t["q"], t["qd"], t["u"], t["qdd"],
+                                                                            t["minv"], stream=stream)),
+        "gradient_knots (77-float records)": (84 + 224 + 392, lambda t: ctx.gradient_knots(n, t["knots"], t["dqdd"],
+                                                                                         stream=stream)),
+        "discrete_jacobians": (392 + 196 + 784 + 392, lambda t: ctx.discrete_jacobians(n, t["dqdd"], t["minv"], 0.01,
+                                                                                       t["A"], t["B"],
+                                                                                       stream=stream)),
+        "gradient_f64 (verification build)": (1400, lambda t: ctx.gradient_f64(n, t["q64"], t["qd64"], t["u64"],
+                                                                               t["dqdd64"], t["qdd64"], t["minv64"],
+                                                                               stream=stream)),
+    }
+    out = {}
+    for name, (bytes_per_knot, call) in calls.items():
+        reps = 4 if "f64" in name else steps
+        for i in range(FLUSH_SETS):
+            call(sets[i])
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(reps):
+            call(sets[i % FLUSH_SETS])
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[name] = {"us_per_launch": round(ms * 1e3, 2), "knots_per_s": n / (ms * 1e-3),
+                     "bytes_per_knot": bytes_per_knot,
+                     "hbm_frac": bytes_per_knot * n / (ms * 1e-3) / 1e9 / float(peaks["hbm_gbs"])}
+    return {"n": n, "l2": f"flushed ({FLUSH_SETS} rotating batches)", "calls": out}
 
 
 def mix_parity(ctx, torch, sets, n, stream):
@@ -404,6 +464,7 @@ def run_frg(args):
     sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_peak = torch.cuda.get_device_properties(dev).multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
     scaling = plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak)
+    entries = entry_points(ctx, torch, dev, stream, peaks)
 
     # ---- serving: latency at 50 % of saturation, and admission under a 2 GiB pool ----
     served = served_adm = None
@@ -440,6 +501,7 @@ def run_frg(args):
                                      "ms_per_step": statistics.mean(plain_ms)},
             "batched_vs_plain": value / ws / plain_value,
             "plain_scaling": scaling,
+            "entry_points": entries,
             "parity": parity,
             "served": served,
             "served_admission": served_adm,

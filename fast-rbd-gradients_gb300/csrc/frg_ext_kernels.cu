@@ -77,6 +77,61 @@ __global__ void discretize_kernel(int n, const float *dqdd, const float *minv, f
     }
 }
 
+// The same per 64-knot chunk, for 16-byte-aligned arrays.  The chunk's dqdd
+// and Minv (25,088 B and 12,544 B) are staged in shared memory with 16-byte
+// loads; A and B leave as 16-byte stores, coalesced.  Each thread owns one
+// float4 position j of a knot's A (49 float4) and of a knot pair's B (49
+// float4), so the element arithmetic is done once per thread and the loops
+// over the chunk's knots only load, scale and store.  The expressions per
+// element are those of discretize_kernel, so the bits are too.
+constexpr int kDiscKnots = 64;
+__global__ void __launch_bounds__(256) discretize_chunks_kernel(int nchunks, const float *dqdd, const float *minv,
+                                                                float dt, float *A, float *B) {
+    __shared__ float4 s_dqdd4[kDiscKnots * 98 / 4];
+    __shared__ float4 s_minv4[kDiscKnots * 49 / 4];
+    const float *s_dqdd = reinterpret_cast<const float *>(s_dqdd4);
+    const float *s_minv = reinterpret_cast<const float *>(s_minv4);
+    const int ngroups = blockDim.x / 49;  // groups of 49 threads
+    const int g = threadIdx.x / 49, j = threadIdx.x - g * 49;
+    int asrc[4], bsrc[4];  // offset into the knot's dqdd / the knot pair's Minv, or -1
+    float aconst[4], aone[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        const int idx = 4 * j + t, r = idx % 14, c = idx / 14;  // A element (r, c) of 14 x 14
+        asrc[t] = r < 7 ? -1 : (r - 7) + 7 * c;
+        aconst[t] = r < 7 && c == r + 7 ? dt : 0.0f;
+        aone[t] = r == c ? 1.0f : 0.0f;
+        const int kp = idx / 98, bi = idx - kp * 98, br = bi % 14, bc = bi / 14;  // B element of knot kp
+        bsrc[t] = br < 7 ? -1 : 49 * kp + (br - 7) + 7 * bc;
+    }
+    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const long long k0 = static_cast<long long>(ch) * kDiscKnots;
+        const float4 *gd = reinterpret_cast<const float4 *>(dqdd + 98 * k0);
+        const float4 *gm = reinterpret_cast<const float4 *>(minv + 49 * k0);
+        for (int i = threadIdx.x; i < kDiscKnots * 98 / 4; i += blockDim.x) s_dqdd4[i] = __ldg(gd + i);
+        for (int i = threadIdx.x; i < kDiscKnots * 49 / 4; i += blockDim.x) s_minv4[i] = __ldg(gm + i);
+        __syncthreads();
+        if (g < ngroups) {
+            float4 *gA = reinterpret_cast<float4 *>(A + 196 * k0);
+            for (int kk = g; kk < kDiscKnots; kk += ngroups) {
+                float v[4];
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                    v[t] = (asrc[t] >= 0 ? dt * s_dqdd[98 * kk + asrc[t]] : aconst[t]) + aone[t];
+                gA[49 * kk + j] = make_float4(v[0], v[1], v[2], v[3]);
+            }
+            float4 *gB = reinterpret_cast<float4 *>(B + 98 * k0);
+            for (int kp = g; kp < kDiscKnots / 2; kp += ngroups) {
+                float v[4];
+#pragma unroll
+                for (int t = 0; t < 4; t++) v[t] = bsrc[t] >= 0 ? dt * s_minv[98 * kp + bsrc[t]] : 0.0f;
+                gB[49 * kp + j] = make_float4(v[0], v[1], v[2], v[3]);
+            }
+        }
+        __syncthreads();  // the next chunk overwrites the staging
+    }
+}
+
 // status[k] |= bit for every non-finite element of a knot-major array of W
 // floats per knot (element-parallel and coalesced; atomics only on hits).
 template <int W>
@@ -157,10 +212,23 @@ cudaError_t launch_ext(bool damping, bool mpc, const LaunchShape &shape, int n, 
 cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float dt, float *A, float *B,
                               cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
-    const long long total = static_cast<long long>(n) * 294;
-    long long blocks = (total + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    discretize_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(n, dqdd, minv, dt, A, B);
+    auto al16 = [](const void *p) { return (reinterpret_cast<unsigned long long>(p) & 15ull) == 0; };
+    int done = 0;  // knots handled by the chunked kernel
+    if (al16(dqdd) && al16(minv) && al16(A) && al16(B) && n >= kDiscKnots) {
+        const int nchunks = n / kDiscKnots;
+        const int grid = nchunks < 152 * 64 ? nchunks : 152 * 64;
+        discretize_chunks_kernel<<<grid, 256, 0, stream>>>(nchunks, dqdd, minv, dt, A, B);
+        done = nchunks * kDiscKnots;
+    }
+    const int rest = n - done;
+    if (rest > 0) {
+        const long long d = done;
+        const long long total = static_cast<long long>(rest) * 294;
+        long long blocks = (total + 255) / 256;
+        if (blocks > 152 * 16) blocks = 152 * 16;
+        discretize_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(rest, dqdd + 98 * d, minv + 49 * d, dt,
+                                                                        A + 196 * d, B + 98 * d);
+    }
     return cudaGetLastError();
 }
 

@@ -80,6 +80,28 @@ def test_discrete_jacobians():
     assert max_err(Bgot.reshape(n, -1), Bref.reshape(n, -1)) <= TOL
 
 
+def test_discrete_jacobians_chunked_and_elementwise_agree():
+    """16-byte-aligned arrays take the 64-knot chunk kernel (plus an
+    element-wise tail); arrays one float off alignment take the element-wise
+    kernel throughout.  Both give the same bits."""
+    import torch
+    n, dt = 1000, 0.02  # 15 chunks and a tail of 40 knots
+    q, qd, u = frg.sample_knots(n, seed=78)
+    tq, tqd, tu = dev(torch, q, qd, u)
+    d, qq, m = (torch.empty((n, w), device="cuda") for w in (98, 7, 49))
+    A = torch.empty((n, 196), device="cuda")
+    B = torch.empty((n, 98), device="cuda")
+    Abuf = torch.empty(n * 196 + 1, device="cuda")
+    Bbuf = torch.empty(n * 98 + 1, device="cuda")
+    A1, B1 = Abuf[1:].view(n, 196), Bbuf[1:].view(n, 98)
+    with frg.Context() as ctx:
+        ctx.gradient(n, tq, tqd, tu, d, qq, m)
+        ctx.discrete_jacobians(n, d, m, dt, A, B)
+        ctx.discrete_jacobians(n, d, m, dt, A1, B1)
+        torch.cuda.synchronize()
+    assert torch.equal(A, A1) and torch.equal(B, B1)
+
+
 @pytest.mark.parametrize("damping,mpc", [(0, 0), (1, 1)])
 @pytest.mark.parametrize("n", [1, 33, 1000])
 def test_gradient_over_reference_knot_records(damping, mpc, n):
