@@ -97,9 +97,12 @@ __device__ __forceinline__ void next_element(int &kn, int &j) {
 
 // Gather of W reals per knot (knot-major) into stage[lane*W + j].  Tiles of
 // one run copy their n*W reals straight and coalesced (16-byte slots when the
-// run is 32 knots and aligned); idle lanes get zeros.
+// run is 32 knots and aligned); idle lanes get zeros.  Other tiles (knots of
+// several trajectories, strided records) read element by element through the
+// knots' pointers in the warp's table (see scatter_out), coalesced: first all
+// pointers, then all W loads in flight, then the shared-memory stores.
 template <int W>
-__device__ __forceinline__ void gather_in(real *stage, const real *base, int lane) {
+__device__ __forceinline__ void gather_in(real *stage, const real *base, int lane, const real **knot) {
     const real *b0;
     const int n = tile_run<W>(base, lane, b0);
     if (n == 32 && aligned16(b0)) {
@@ -115,10 +118,27 @@ __device__ __forceinline__ void gather_in(real *stage, const real *base, int lan
         for (int e = lane; e < 32 * W; e += 32) stage[e] = e < lim ? __ldg(b0 + e) : real(0);
         return;
     }
-    // Other tiles (knots of several trajectories, idle lanes, strided
-    // records): each lane reads its own knot, all W loads in flight at once.
+    if constexpr (W <= 7) {
+        knot[lane] = base;
+        __syncwarp();
+        int kn = lane / W, j = lane % W;
+        const real *p[W];
 #pragma unroll
-    for (int j = 0; j < W; j++) stage[lane * W + j] = base ? __ldg(base + j) : real(0);
+        for (int m = 0; m < W; m++) {
+            p[m] = knot[kn];
+            if (p[m]) p[m] += j;
+            next_element<W>(kn, j);
+        }
+        real v[W];
+#pragma unroll
+        for (int m = 0; m < W; m++) v[m] = p[m] ? __ldg(p[m]) : real(0);
+        __syncwarp();  // every lane has read the table
+#pragma unroll
+        for (int m = 0; m < W; m++) stage[lane + 32 * m] = v[m];
+    } else {  // wider knots (external forces): each lane reads its own, all loads in flight
+#pragma unroll
+        for (int j = 0; j < W; j++) stage[lane * W + j] = base ? __ldg(base + j) : real(0);
+    }
 }
 
 // Scatter of stage[lane*W + j] to each knot's W reals at base (knots STRIDE
@@ -716,9 +736,9 @@ template <bool DAMP, bool MPC, bool MIRROR = false, bool FEXT = false, bool FDON
 __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotPtrs &kp,
                                              const KnotPtrs &mr = KnotPtrs{}) {
     real q[7], qd[7], u[7];
-    gather_in<7>(ws->stage, kp.q, lane);
-    gather_in<7>(ws->stage + 224, kp.qd, lane);
-    gather_in<7>(ws->stage + 448, kp.u, lane);
+    gather_in<7>(ws->stage, kp.q, lane, ws->knot);
+    gather_in<7>(ws->stage + 224, kp.qd, lane, ws->knot);
+    gather_in<7>(ws->stage + 448, kp.u, lane, ws->knot);
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < 7; j++) {
@@ -734,7 +754,7 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     }
     const real *fx = nullptr;
     if constexpr (FEXT) {  // the lane's 42 external-force values stay staged through both RNEA passes
-        gather_in<42>(ws->stage, kp.fext, lane);
+        gather_in<42>(ws->stage, kp.fext, lane, ws->knot);
         __syncwarp();
         fx = ws->stage + lane * 42;
     }
