@@ -163,6 +163,11 @@ frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s)
         }
         return ms_min;
     };
+    // A candidate replaces the best only when more than 1 % faster: near-ties
+    // keep the earlier candidate, and each CTA size is tried at full residency
+    // first.  On the tuning batch (whole tiles) shapes with fewer resident warps
+    // can tie the full ones, but on batches with split tiles they are slower.
+    constexpr float kMargin = 0.99f;
     // 1) contiguous batches: the plain kernel (threads per knot x warps per CTA)
     frg::LaunchShape best = saved;
     float best_ms = FLT_MAX;
@@ -172,7 +177,7 @@ frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s)
             ctx->shape.warps_per_cta = w;
             ctx->shape.lanes_per_knot = lanes;
             const float ms = time_ms([&] { return frg_launch_whole(ctx, tr, s); });
-            if (ms < best_ms) {
+            if (ms < best_ms * kMargin) {
                 best_ms = ms;
                 best = ctx->shape;
             }
@@ -206,7 +211,7 @@ frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s)
                 ctx->ragged_shape.ctas_per_sm = c;
                 ctx->ragged_shape.lanes_per_knot = lanes;
                 const float ms = time_ms([&] { return frg_launch_batch(ctx, ds, nseg, ntiles_s, s); });
-                if (ms < best_r_ms) {
+                if (ms < best_r_ms * kMargin) {
                     best_r_ms = ms;
                     best_r = ctx->ragged_shape;
                 }
