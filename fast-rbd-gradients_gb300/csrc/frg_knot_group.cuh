@@ -129,10 +129,19 @@ __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const Kno
         u[j] = kp.q ? __ldg(kp.u + j) : 0.0f;
     }
     if constexpr (MIRROR) {
-        if (mr.q && g < 7) {
-            const_cast<float *>(mr.q)[g] = q[g];
-            const_cast<float *>(mr.qd)[g] = qd[g];
-            const_cast<float *>(mr.u)[g] = u[g];
+        if (mr.q && g < 7) {  // entry g, picked with compile-time indices (no local-memory arrays)
+            float qg = q[0], qdg = qd[0], ug = u[0];
+#pragma unroll
+            for (int j = 1; j < 7; j++) {
+                if (j == g) {
+                    qg = q[j];
+                    qdg = qd[j];
+                    ug = u[j];
+                }
+            }
+            const_cast<float *>(mr.q)[g] = qg;
+            const_cast<float *>(mr.qd)[g] = qdg;
+            const_cast<float *>(mr.u)[g] = ug;
         }
     }
     float sq[7], cq[7];
