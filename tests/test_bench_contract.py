@@ -1,0 +1,66 @@
+"""bench.py's contract on CPU: the reference arm's JSON line (the reference
+algorithm's CPU path on this host), its rank handling under torchrun, and the
+helpers the GPU arm's line is built from (the ncu traffic figure read from the
+committed profile, the measured peaks)."""
+import json
+import os
+import subprocess
+import sys
+
+from conftest import ROOT
+
+BENCH = os.path.join(ROOT, "bench.py")
+
+
+def _run(args, env_extra=None):
+    env = dict(os.environ)
+    env.update(env_extra or {})
+    return subprocess.run([sys.executable, BENCH] + args, capture_output=True, text=True, env=env, cwd=ROOT,
+                          timeout=600)
+
+
+def test_reference_arm_prints_the_contract_line():
+    r = _run(["--impl", "reference", "--steps", "2", "--warmup", "1"])
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["steps"] == 2 and d["warmup"] == 1 and d["n_gpus"] == 1
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["vs_baseline"] is None
+    assert d["unit"] == "knot-gradients/s" and d["scaling"] == "weak"
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["unit"] == d["unit"] and cb["cores"] >= 1
+    assert cb["kind"] in ("port", "reference") and isinstance(cb["sample"], str)
+    e2e = d["e2e"]
+    assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    assert d["config"]["knots_per_step"] == 66809
+
+
+def test_reference_arm_other_ranks_do_no_work():
+    r = _run(["--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1"],
+             {"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip() == ""
+
+
+def test_profile_traffic_figure_parses():
+    """The GPU arm's roofline `traffic` is this figure x knots per launch; it must
+    parse and lie between the algorithmic input bytes and twice the algorithmic total."""
+    sys.path.insert(0, ROOT)
+    import bench
+    t = bench.ncu_traffic_per_knot()
+    assert t is not None and 84 < t < 2 * bench.BYTES_PER_KNOT
+
+
+def test_peaks_are_read_from_the_measured_file():
+    sys.path.insert(0, ROOT)
+    import bench
+    peaks, src = bench.load_peaks()
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        assert src == "measured"
+    assert float(peaks["hbm_gbs"]) > 0
