@@ -525,15 +525,25 @@ frg_status frg_server_poll(frg_server *s, uint64_t request_id, frg_request_info 
 frg_status frg_server_wait(frg_server *s, uint64_t request_id, int64_t timeout_us, frg_request_info *info) {
     if (!s) return FRG_ERR_INVALID_ARGUMENT;
     std::unique_lock<std::mutex> lk(s->mu);
-    auto it = s->reqs.find(request_id);
-    if (it == s->reqs.end() || it->second->consumed) return FRG_ERR_NOT_FOUND;
-    Request *r = it->second.get();
-    auto done = [&] { return r->state == ReqState::Done; };
-    if (timeout_us < 0) s->cv_done.wait(lk, done);
-    else if (!s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), done)) {
-        fill_info(s, *r, info);
+    // The request is looked up by id on every wake-up: while this thread
+    // sleeps, a concurrent poll / wait_any may take the same completion and
+    // free the request, so no pointer to it is held across the wait.
+    auto live = [&]() -> Request * {
+        auto it = s->reqs.find(request_id);
+        return it == s->reqs.end() || it->second->consumed ? nullptr : it->second.get();
+    };
+    if (!live()) return FRG_ERR_NOT_FOUND;
+    auto settled = [&] {
+        const Request *r = live();
+        return !r || r->state == ReqState::Done;
+    };
+    if (timeout_us < 0) s->cv_done.wait(lk, settled);
+    else if (!s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), settled)) {
+        if (const Request *r = live()) fill_info(s, *r, info);
         return FRG_ERR_TIMEOUT;
     }
+    Request *r = live();
+    if (!r) return FRG_ERR_NOT_FOUND;  // taken by another thread while this one waited
     fill_info(s, *r, info);
     r->consumed = true;
     s->reqs.erase(request_id);
