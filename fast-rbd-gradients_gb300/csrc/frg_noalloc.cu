@@ -25,7 +25,7 @@
 
 #include "frg.h"
 #include "frg_internal.h"
-#include "frg_knot.cuh"
+#include "frg_kernels.cuh"
 
 namespace {
 
@@ -51,66 +51,19 @@ std::mutex g_mu;  // guards the host staging and the per-device set-up table
 constexpr int kMaxDevices = 64;
 unsigned char *g_dev_scratch[kMaxDevices] = {};
 
-// Same work as the batched kernel (frg_kernels.cu), with its descriptor lists
-// and counter taken from the static scratch.
-template <bool DAMP, bool MPC>
-__global__ void __launch_bounds__(8 * 32)
-    grad_ragged_noalloc_kernel(const frg::Segment *segs, int nseg, const int *tile_seg, int ntiles,
-                               unsigned int *counter) {
-    extern __shared__ float4 smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    frg::WarpSmem *ws = reinterpret_cast<frg::WarpSmem *>(smem_raw) + warp;
-    const unsigned int total_warps = gridDim.x * (blockDim.x >> 5);
-    for (;;) {
-        unsigned int ticket = 0;
-        if (lane == 0) ticket = atomicAdd(counter, 1u);
-        ticket = __shfl_sync(0xffffffffu, ticket, 0);
-        if (ticket >= static_cast<unsigned int>(ntiles)) {
-            if (lane == 0 && ticket == static_cast<unsigned int>(ntiles) + total_warps - 1u) atomicExch(counter, 0u);
-            return;
-        }
-        const long long g = static_cast<long long>(ticket) * 32 + lane;
-        frg::KnotPtrs kp{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-        if (g < segs[nseg].knot_begin) {
-            int s = tile_seg[ticket];
-            while (s + 1 < nseg && segs[s + 1].knot_begin <= g) s++;
-            const frg::Segment &sg = segs[s];
-            const long long i = g - sg.knot_begin;
-            kp = frg::KnotPtrs{sg.q + 7 * i, sg.qd + 7 * i, sg.u + 7 * i, sg.dqdd + 98 * i, sg.qdd + 7 * i,
-                               sg.minv + 49 * i};
-        }
-        frg::process_tile<DAMP, MPC>(ws, lane, kp);
-    }
-}
-
-template <bool D, bool M>
-cudaError_t set_smem() {
-    return cudaFuncSetAttribute(grad_ragged_noalloc_kernel<D, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(sizeof(frg::WarpSmem)) * 8);
-}
-
-// Once per device, with that device current: the scratch's device address and
-// the kernels' shared-memory opt-in.  Caller holds g_mu.
+// Once per device, with that device current: the scratch's device address.
+// (The persistent kernels' shared-memory opt-in is part of frg_create.)
+// Caller holds g_mu.
 cudaError_t device_setup(int device, unsigned char **out) {
     if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
     if (!g_dev_scratch[device]) {
         unsigned char *ptr = nullptr;
         cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&ptr), g_noalloc_scratch);
         if (e != cudaSuccess) return e;
-        for (cudaError_t r : {set_smem<false, false>(), set_smem<true, false>(), set_smem<false, true>(),
-                              set_smem<true, true>()})
-            if (r != cudaSuccess) return r;
         g_dev_scratch[device] = ptr;
     }
     *out = g_dev_scratch[device];
     return cudaSuccess;
-}
-
-template <bool D, bool M>
-void launch(int grid, int warps, const frg::Segment *segs, int nseg, const int *tile_seg, int ntiles,
-            unsigned int *counter, cudaStream_t st) {
-    grad_ragged_noalloc_kernel<D, M><<<grid, warps * 32, sizeof(frg::WarpSmem) * warps, st>>>(segs, nseg, tile_seg,
-                                                                                               ntiles, counter);
 }
 
 }  // namespace
@@ -185,15 +138,12 @@ extern "C" frg_status frg_gradient_ragged_noalloc(frg_ctx *ctx, int n_traj, cons
         frg_set_error(ctx, std::string("frg_gradient_ragged_noalloc upload: ") + cudaGetErrorString(e));
         return FRG_ERR_CUDA;
     }
-    const int warps = ctx->shape.warps_per_cta;
-    int grid = ctx->num_sms * ctx->shape.ctas_per_sm;
-    const int needed = (ntiles + warps - 1) / warps;
-    if (grid > needed) grid = needed;
-    if (ctx->damping && ctx->mpc) launch<true, true>(grid, warps, segs, n_traj, tile_seg, ntiles, counter, st);
-    else if (ctx->damping) launch<true, false>(grid, warps, segs, n_traj, tile_seg, ntiles, counter, st);
-    else if (ctx->mpc) launch<false, true>(grid, warps, segs, n_traj, tile_seg, ntiles, counter, st);
-    else launch<false, false>(grid, warps, segs, n_traj, tile_seg, ntiles, counter, st);
-    if ((e = cudaGetLastError()) != cudaSuccess) {
+    // the batched path's persistent kernels, at the context's tuned persistent
+    // shape and mapping, with descriptors and counter in the static scratch
+    e = frg::launch_ragged(ctx->damping, ctx->mpc, ctx->ragged_shape, ctx->num_sms, segs, n_traj, tile_seg, ntiles,
+                           counter, st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
         frg_set_error(ctx, std::string("frg_gradient_ragged_noalloc launch: ") + cudaGetErrorString(e));
         return FRG_ERR_CUDA;
     }

@@ -110,6 +110,23 @@ frg_status frg_gradient(frg_ctx *ctx, int n_knots, const float *q, const float *
                         float *qdd, float *minv, frg_stream stream);
 
 /*
+ * Single-knot latency, the counterpart of the reference's kern_single_full
+ * (time_GPU.cu:23-51, timed at :191-195), which repeats one knot TEST_ITERS
+ * times inside one CTA so that the time per knot excludes the launch.  Here
+ * one warp carries ONE knot (q, qd, u [7], DEVICE) through the whole path
+ * `iters` times in a row in one launch -- each repetition exactly as a
+ * one-knot frg_gradient does it, results stored to dqdd [98], qdd [7],
+ * minv [49] -- in the thread mapping lanes_per_knot (1: one lane; 8: eight
+ * lanes share the knot's columns, the mapping small batches use).
+ * Asynchronous on `stream`; with us_per_knot != NULL it waits for the launch
+ * and writes its CUDA-event time divided by iters (launch included, so use a
+ * large iters, or the difference of two iters, to take the launch out).
+ */
+frg_status frg_single_knot_latency(frg_ctx *ctx, int lanes_per_knot, int iters, const float *q, const float *qd,
+                                   const float *u, float *dqdd, float *qdd, float *minv, frg_stream stream,
+                                   double *us_per_knot);
+
+/*
  * Same, for HOST arrays, synchronous: returns when the results are in the host
  * arrays (the time_GPU.cu:313-316 "Compute + I/O" sequence).  Pinned arrays
  * (frg_host_alloc, cudaHostAlloc / cudaHostRegister) take a single launch
@@ -217,7 +234,7 @@ frg_status frg_gradient_ragged(frg_ctx *ctx, int n_traj, const int64_t *offsets,
  * that every GPU loading the library holds until process exit, so at most
  * FRG_NOALLOC_MAX_TRAJ trajectories and FRG_NOALLOC_MAX_KNOTS knots per call
  * (larger batches return FRG_ERR_INVALID_ARGUMENT).  The first call on a
- * device looks up that array's device address and sets the kernel up: make it
+ * device looks up that array's device address on that device: make it
  * before any stream capture.  All calls share the array: calls whose launches
  * may overlap on the GPU (different streams, unordered) race -- order them.
  */
