@@ -290,6 +290,39 @@ frg_status frg_gradient(frg_ctx *ctx, int n_knots, const float *q, const float *
     return FRG_OK;
 }
 
+frg_status frg_single_knot_latency(frg_ctx *ctx, int lanes_per_knot, int iters, const float *q, const float *qd,
+                                   const float *u, float *dqdd, float *qdd, float *minv, frg_stream stream,
+                                   double *us_per_knot) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if ((lanes_per_knot != 1 && lanes_per_knot != 8) || iters < 1 || !(q && qd && u && dqdd && qdd && minv)) {
+        frg_set_error(ctx, "frg_single_knot_latency: lanes_per_knot must be 1 or 8, iters >= 1, arrays non-null");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    DeviceGuard g(ctx->device);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (us_per_knot) {
+        if (!check(ctx, cudaEventCreate(&e0), "cudaEventCreate") || !check(ctx, cudaEventCreate(&e1), "cudaEventCreate") ||
+            !check(ctx, cudaEventRecord(e0, stream), "cudaEventRecord")) {
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            return FRG_ERR_CUDA;
+        }
+    }
+    bool ok = check(ctx, frg::launch_single_knot(ctx->damping, ctx->mpc, lanes_per_knot, iters, q, qd, u, dqdd, qdd,
+                                                 minv, stream),
+                    "frg_single_knot_latency launch");
+    if (us_per_knot) {
+        float ms = 0.0f;
+        ok = ok && check(ctx, cudaEventRecord(e1, stream), "cudaEventRecord") &&
+             check(ctx, cudaEventSynchronize(e1), "cudaEventSynchronize") &&
+             check(ctx, cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        if (ok) *us_per_knot = 1e3 * static_cast<double>(ms) / iters;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    return ok ? FRG_OK : FRG_ERR_CUDA;
+}
+
 frg_status frg_gradient_fext(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
                              const float *fext, float *dqdd, float *qdd, float *minv, frg_stream stream) {
     if (!fext) return frg_gradient(ctx, n_knots, q, qd, u, dqdd, qdd, minv, stream);

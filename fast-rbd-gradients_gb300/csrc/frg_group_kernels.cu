@@ -32,6 +32,23 @@ __global__ void __launch_bounds__(kMaxWarps * 32)
         process_group<DAMP, MPC>(gs, lane, plain_group_knot(q, qd, u, dqdd, qdd, minv, n, it, lane));
 }
 
+// Single-knot latency in this mapping: one warp, knot slot 0 (lanes 0-7)
+// carries one knot through the whole path `iters` times; the (i & zero) knot
+// offset keeps every repetition in the loop (see grad_single_knot_kernel).
+template <bool DAMP, bool MPC>
+__global__ void __launch_bounds__(32)
+    grad_group_single_knot_kernel(const float *q, const float *qd, const float *u, float *dqdd, float *qdd,
+                                  float *minv, int iters, int zero) {
+    extern __shared__ float4 smem_raw[];
+    const int lane = threadIdx.x & 31;
+    GroupSmem *gs = reinterpret_cast<GroupSmem *>(smem_raw);
+    for (int i = 0; i < iters; i++) {
+        const long long o = static_cast<long long>(i & zero);
+        process_group<DAMP, MPC>(gs, lane, plain_group_knot(q + 7 * o, qd + 7 * o, u + 7 * o, dqdd + 98 * o,
+                                                            qdd + 7 * o, minv + 49 * o, 1, 0, lane));
+    }
+}
+
 // persistent: ticket -> (32-knot tile t, 4-knot slice s); the last ticket
 // (items + total_warps - 1) resets the counter, as in grad_ragged_kernel
 template <bool DAMP, bool MPC, bool SERVE, typename Seg>
@@ -140,6 +157,16 @@ cudaError_t launch_group_plain(bool damping, bool mpc, const LaunchShape &sh, in
     const int grid = static_cast<int>((items + w - 1) / w);
     const size_t smem = sizeof(GroupSmem) * w;
 #define FRG_CALL(D, M) grad_group_plain_kernel<D, M><<<grid, w * 32, smem, st>>>(q, qd, u, dqdd, qdd, minv, n);
+    FRG_DISPATCH(damping, mpc, FRG_CALL)
+#undef FRG_CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_group_single_knot(bool damping, bool mpc, int iters, const float *q, const float *qd,
+                                     const float *u, float *dqdd, float *qdd, float *minv, cudaStream_t st) {
+    if (iters <= 0) return cudaSuccess;
+    const size_t smem = sizeof(GroupSmem);
+#define FRG_CALL(D, M) grad_group_single_knot_kernel<D, M><<<1, 32, smem, st>>>(q, qd, u, dqdd, qdd, minv, iters, 0);
     FRG_DISPATCH(damping, mpc, FRG_CALL)
 #undef FRG_CALL
     return cudaGetLastError();

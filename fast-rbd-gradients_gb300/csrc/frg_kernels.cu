@@ -107,6 +107,27 @@ __global__ void __launch_bounds__(kMaxWarpsPerCta * 32)
     }
 }
 
+// Single-knot latency (the reference's kern_single_full, time_GPU.cu:23-51,
+// which repeats one knot TEST_ITERS times inside one CTA): one warp carries
+// one knot (lane 0) through the whole path `iters` times in a row, each time
+// exactly as a one-knot launch does -- gather, arithmetic, scatter of every
+// result.  Repetition i reads the knot at an offset of (i & zero) knots;
+// `zero` is 0 at run time, but the compiler cannot know it, so no repetition
+// can be hoisted out of the loop.
+template <bool DAMP, bool MPC>
+__global__ void __launch_bounds__(32) grad_single_knot_kernel(PlainArgs a, int iters, int zero) {
+    extern __shared__ float4 smem_raw[];
+    const int lane = threadIdx.x & 31;
+    WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw);
+    for (int i = 0; i < iters; i++) {
+        const long long o = static_cast<long long>(i & zero);
+        const KnotPtrs kp = lane == 0 ? KnotPtrs{a.q + 7 * o, a.qd + 7 * o, a.u + 7 * o, a.dqdd + 98 * o,
+                                                 a.qdd + 7 * o, a.minv + 49 * o}
+                                      : KnotPtrs{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+        process_tile<DAMP, MPC>(ws, lane, kp);
+    }
+}
+
 template <typename K>
 cudaError_t prepare(K kernel) {
     static_assert(sizeof(WarpSmem) % 16 == 0, "warp smem must keep float4 alignment");
@@ -192,6 +213,21 @@ cudaError_t launch_host_out(bool damping, bool mpc, const LaunchShape &shape, in
     if (damping && !mpc) return plain_impl<true, false, true>(shape, a, stream);
     if (!damping && mpc) return plain_impl<false, true, true>(shape, a, stream);
     return plain_impl<true, true, true>(shape, a, stream);
+}
+
+cudaError_t launch_single_knot(bool damping, bool mpc, int lanes_per_knot, int iters, const float *q,
+                               const float *qd, const float *u, float *dqdd, float *qdd, float *minv,
+                               cudaStream_t stream) {
+    if (iters <= 0) return cudaSuccess;
+    if (lanes_per_knot == 8) return launch_group_single_knot(damping, mpc, iters, q, qd, u, dqdd, qdd, minv, stream);
+    if (lanes_per_knot != 1) return cudaErrorInvalidValue;
+    const PlainArgs a{q, qd, u, dqdd, qdd, minv, 1};
+    const size_t smem = sizeof(WarpSmem);
+    if (!damping && !mpc) grad_single_knot_kernel<false, false><<<1, 32, smem, stream>>>(a, iters, 0);
+    else if (damping && !mpc) grad_single_knot_kernel<true, false><<<1, 32, smem, stream>>>(a, iters, 0);
+    else if (!damping && mpc) grad_single_knot_kernel<false, true><<<1, 32, smem, stream>>>(a, iters, 0);
+    else grad_single_knot_kernel<true, true><<<1, 32, smem, stream>>>(a, iters, 0);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_ragged(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const Segment *segs,

@@ -66,6 +66,12 @@ cudaError_t launch_serve(bool damping, bool mpc, const LaunchShape &shape, int n
                          int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream);
 cudaError_t init_serve_kernels();
 
+// Single-knot latency: one warp repeats the whole path over ONE knot `iters`
+// times in one launch (lanes_per_knot 1 or 8 selects the thread mapping).
+cudaError_t launch_single_knot(bool damping, bool mpc, int lanes_per_knot, int iters, const float *q,
+                               const float *qd, const float *u, float *dqdd, float *qdd, float *minv,
+                               cudaStream_t stream);
+
 // Latency mapping (8 lanes per knot), same arguments as the launches above.
 cudaError_t init_group_kernels();
 size_t group_warp_smem_bytes();
@@ -73,6 +79,8 @@ int max_group_ctas_per_sm(int warps);
 cudaError_t launch_group_plain(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q,
                                const float *qd, const float *u, float *dqdd, float *qdd, float *minv,
                                cudaStream_t stream);
+cudaError_t launch_group_single_knot(bool damping, bool mpc, int iters, const float *q, const float *qd,
+                                     const float *u, float *dqdd, float *qdd, float *minv, cudaStream_t stream);
 cudaError_t launch_group_ragged(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const Segment *segs,
                                 int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream);
 cudaError_t launch_group_serve(bool damping, bool mpc, const LaunchShape &shape, int num_sms, const ServeSegment *segs,

@@ -36,6 +36,7 @@ EXPORTED = (
     "frg_server_wait_any", "frg_server_release", "frg_server_get_stats", "frg_gradient_fext",
     "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64", "frg_get_tuning",
     "frg_set_tuning", "frg_knot_status", "frg_model_name", "frg_gradient_knots", "frg_server_cancel",
+    "frg_single_knot_latency",
 )
 
 KNOT_NONFINITE_INPUT = 1
@@ -139,6 +140,7 @@ def _declare(L):
         "frg_knot_status": (st, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
         "frg_model_name": (ctypes.c_char_p, []),
         "frg_gradient_knots": (st, [vp, i32, vp, vp, vp]),
+        "frg_single_knot_latency": (st, [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -298,6 +300,16 @@ class Context:
         """Plain path on device buffers (addresses, torch tensors)."""
         self._check(lib().frg_gradient(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd), _ptr(qdd),
                                        _ptr(minv), _stream_ptr(stream)), "frg_gradient")
+
+    def single_knot_latency(self, lanes_per_knot, iters, q, qd, u, dqdd, qdd, minv, stream=None, timed=False):
+        """One knot (device arrays) through the whole path `iters` times in one
+        launch; with timed=True waits and returns µs per repetition (CUDA events,
+        launch included)."""
+        us = ctypes.c_double(0.0)
+        self._check(lib().frg_single_knot_latency(self._h, int(lanes_per_knot), int(iters), _ptr(q), _ptr(qd), _ptr(u),
+                                                  _ptr(dqdd), _ptr(qdd), _ptr(minv), _stream_ptr(stream),
+                                                  ctypes.byref(us) if timed else None), "frg_single_knot_latency")
+        return us.value if timed else None
 
     def gradient_fext(self, n_knots, q, qd, u, fext, dqdd, qdd, minv, stream=None):
         """Gradient with external link forces fext [n][7][6] (device buffers)."""
