@@ -53,7 +53,45 @@ def test_edge_horizons(horizons):
     if n:
         rd, rq, rm = frg_oracle.gradient_f64(q[:n], qd[:n], u[:n])
         assert max_err(out[0].cpu().numpy()[:n], rd) <= TOL
+        assert max_err(out[1].cpu().numpy()[:n], rq) <= TOL
         assert max_err(out[2].cpu().numpy()[:n], rm) <= TOL
+
+
+@pytest.mark.parametrize("damping,mpc", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_full_mix_every_knot_vs_oracle(damping, mpc):
+    """The benchmark's workload, every knot: the 512-trajectory mix (seed 2021,
+    66,809 knots) stored in shuffled order, so a plan runs the persistent
+    kernel over scattered trajectories; all of dqdd, q̈ and Minv of every knot
+    against the FP64 CPU oracle."""
+    import torch
+    h, off = frg.ragged_horizons(512, 8, 256, seed=2021)
+    n = int(off[-1])
+    q, qd, u = frg.sample_knots(n, seed=2022)
+    perm = np.random.Generator(np.random.PCG64(2021)).permutation(512)
+    mem_off = np.zeros(512, np.int64)
+    pos = 0
+    for t in perm:
+        mem_off[t] = pos
+        pos += int(h[t])
+    # knot k of trajectory t sits at memory row mem_off[t] + k
+    rows = np.concatenate([mem_off[t] + np.arange(h[t]) for t in range(512)])
+    tq, tqd, tu = (torch.from_numpy(np.ascontiguousarray(x[np.argsort(rows)])).cuda() for x in (q, qd, u))
+    out = [torch.full((n, w), float("nan"), device="cuda") for w in (98, 7, 49)]
+    with frg.Context(vel_damping=bool(damping), mpc_mode=bool(mpc)) as ctx:
+        o = [int(x) for x in mem_off]
+        trajs = [(int(h[t]), tq[o[t]:], tqd[o[t]:], tu[o[t]:], out[0][o[t]:], out[1][o[t]:], out[2][o[t]:])
+                 for t in range(512)]
+        plan = ctx.plan(trajs)
+        try:
+            plan.launch()
+            torch.cuda.synchronize()
+        finally:
+            plan.close()
+    got = [x.cpu().numpy()[rows] for x in out]  # back to trajectory order
+    ref = frg_oracle.gradient_f64(q, qd, u, damping=bool(damping), mpc=bool(mpc))
+    for name, a, r in zip(("dqdd", "qdd", "minv"), got, ref):
+        assert np.isfinite(a).all(), f"{name}: unwritten knots"
+        assert max_err(a, r) <= TOL, name
 
 
 def test_scattered_trajectories_alone_and_in_mix():
