@@ -11,6 +11,11 @@ for p in (os.path.join(ROOT, "fast-rbd-gradients_gb300"), os.path.join(ROOT, "or
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "iiwa_golden.npz")
 
+# The reference tree, read by the tests that regenerate fixtures from it
+# (they skip where it is absent, e.g. on GPU hosts): FRG_REFERENCE_DIR, else
+# its path in the build container.
+REFERENCE_DIR = os.environ.get("FRG_REFERENCE_DIR", "/root/reference")
+
 # Parity bar: max Frobenius-relative error per output matrix and knot against
 # the FP64 oracle / the reference's own FP64 outputs.
 TOL = 1e-4

@@ -6,11 +6,11 @@ import os
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import REFERENCE_DIR, ROOT
 from frg import urdf
 from model_helpers import NewtonEuler, build_oracle, oracle_gradient_f64, synthetic_urdf, write_tables
 
-IIWA_URDF = "/root/reference/utils/iiwa_14.urdf"
+IIWA_URDF = os.path.join(REFERENCE_DIR, "utils", "iiwa_14.urdf")
 IIWA_HEADER = os.path.join(ROOT, "fast-rbd-gradients_gb300", "csrc", "frg_model_iiwa14.h")
 
 
