@@ -100,16 +100,24 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-def ncu_traffic_per_knot():
-    """DRAM bytes per knot of the batched kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "grad_ragged_kernel_mix512.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_knot:"):
-                return float(line.split(":")[1])
-    except OSError:
-        pass
-    return None
+# Figures of one ncu capture of grad_ragged_kernel on this exact workload (the
+# 512-trajectory mix, 66,809 knots, --profile shape), per launch; the command
+# and its full output summary are in profiles/grad_ragged_kernel_bench_mix.md.
+#  - DRAM bytes read + written while the kernel runs: the mix's 41 MB of
+#    results stay dirty in the 129 MB L2 when it ends (written back later, by
+#    the next launches' evictions), so writes are almost absent here;
+#  - FP32 operations executed (2 x FFMA + FADD + FMUL, thread level), which
+#    count what the kernel does after dropping the reference's structural zeros.
+NCU_MIX = {"dram_read_bytes": 6.019e6, "dram_write_bytes": 0.260e6,
+           "l2_write_bytes_all_sources": 77.3e6,
+           "executed_flop_per_knot": 13440.0,
+           "knots": 66809}
+# FP32 CUDA-core peak measured on a GB300 of this machine: every thread of
+# 2 x 1024-thread CTAs per SM runs 8 independent FMA chains (CUDA events, best
+# of 20 launches of 20 ms, SM clock 2070 MHz, no throttle reason): 78.5 TFLOP/s
+# with scalar FFMA, 80.4 with packed FFMA2 (fma.rn.f32x2); the larger is the
+# denominator.  Method and figures in profiles/fp32_fma_peak.md.
+FP32_PEAK_TFLOPS_MEASURED = 80.4
 
 
 class ClockSampler:
@@ -208,6 +216,56 @@ def plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak, steps=20):
                     "hbm_frac": BYTES_PER_KNOT * n / (ms * 1e-3) / 1e9 / float(peaks["hbm_gbs"]),
                     "fp32_frac": FLOP_PER_KNOT_REF * n / (ms * 1e-3) / 1e12 / fp32_peak})
     ctx.set_tuning(saved)
+    return out
+
+
+def host_link_rates(torch, dev, stream, nbytes, reps=10):
+    """Host link rates (GB/s) of plain copies between pinned host memory and
+    device memory, nbytes each, CUDA events on `stream`: the bound of calls
+    whose inputs and results live in host memory."""
+    n = nbytes // 4
+    h = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    d = torch.empty(n, dtype=torch.float32, device=dev)
+    out = {}
+    for name, (dst, src) in (("h2d_gbs", (d, h)), ("d2h_gbs", (h, d))):
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                dst.copy_(src, non_blocking=True)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                dst.copy_(src, non_blocking=True)
+            e1.record(stream)
+        stream.synchronize()
+        out[name] = nbytes * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    return out
+
+
+def single_knot(ctx, torch, dev, stream, n1=100, n2=1100, reps=5):
+    """Single-knot latency (the reference's kern_single_full, time_GPU.cu:23-51):
+    one warp repeats the whole path over one knot inside one launch
+    (frg_single_knot_latency).  us_per_knot is the slope of the CUDA-event time
+    between n1 and n2 repetitions, so the launch is excluded; us_one_repetition
+    is one repetition per launch, launch included."""
+    import frg
+    q, qd, u = (torch.from_numpy(x).to(dev) for x in frg.sample_knots(1, seed=11))
+    outs = [torch.empty((1, w), device=dev) for w in (98, 7, 49)]
+    out = {}
+    for lanes in (1, 8):
+        def per_launch_ms(iters, count):
+            for _ in range(2):
+                ctx.single_knot_latency(lanes, iters, q, qd, u, *outs, stream=stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(count):
+                ctx.single_knot_latency(lanes, iters, q, qd, u, *outs, stream=stream)
+            e1.record(stream)
+            stream.synchronize()
+            return e0.elapsed_time(e1) / count
+        t1, t2 = per_launch_ms(n1, reps), per_launch_ms(n2, reps)
+        out[f"lanes_per_knot_{lanes}"] = {"us_per_knot": (t2 - t1) * 1e3 / (n2 - n1),
+                                          "us_one_repetition": per_launch_ms(1, 50) * 1e3,
+                                          "repetitions": [n1, n2]}
     return out
 
 
@@ -411,7 +469,8 @@ def run_frg(args):
     clocks = ClockSampler(dev.index)
     clocks.start()
     i, tw = 0, time.perf_counter()
-    while i < args.warmup or time.perf_counter() - tw < 1.5:
+    load_window_s = 0.0 if args.profile else 1.5  # profiling: W warm-up launches only
+    while i < args.warmup or time.perf_counter() - tw < load_window_s:
         sets[i % ROTATING_SETS][4].launch(stream)
         i += 1
         if i % 64 == 0:
@@ -460,11 +519,13 @@ def run_frg(args):
     for p in [hq, hqd, hu] + hout:
         frg.lib().frg_host_free(p)
 
+    link = host_link_rates(torch, dev, stream, 616 * n)
+
     # ---- plain path scaling (one launch per batch of N knots) ----
-    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
-    fp32_peak = torch.cuda.get_device_properties(dev).multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_peak = FP32_PEAK_TFLOPS_MEASURED
     scaling = plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak)
     entries = entry_points(ctx, torch, dev, stream, peaks)
+    latency = single_knot(ctx, torch, dev, stream)
 
     # ---- serving: latency at 50 % of saturation, and admission under a 2 GiB pool ----
     served = served_adm = None
@@ -477,11 +538,10 @@ def run_frg(args):
     if rank == 0:
         launch_ms = statistics.mean(step_ms)
         achieved_gbs = BYTES_PER_KNOT * n / (launch_ms * 1e-3) / 1e9
-        traffic_pk = ncu_traffic_per_knot()
-        sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
-        props = torch.cuda.get_device_properties(dev)
-        fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+        traffic_pk = (NCU_MIX["dram_read_bytes"] + NCU_MIX["dram_write_bytes"]) / NCU_MIX["knots"]
         fp32_achieved = FLOP_PER_KNOT_REF * n / (launch_ms * 1e-3) / 1e12
+        fp32_executed = NCU_MIX["executed_flop_per_knot"] * n / (launch_ms * 1e-3) / 1e12
+        d2h_s = 616 * n / (link["d2h_gbs"] * 1e9)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -496,25 +556,34 @@ def run_frg(args):
                 "autotune_knots_per_s": tuned, "parallelism": f"replicas x{ws} (knots sharded, no collective)",
             },
             "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 84 * n, "d2h_bytes_per_step": 616 * n,
-                    "call": "frg_gradient_host (pinned host buffers)"},
+                    "call": "frg_gradient_host (pinned host buffers)", "ms_per_step": e2e_s * 1e3,
+                    "host_link": dict(link, bound="d2h: results' bytes / measured device-to-host copy rate",
+                                      bound_ms=d2h_s * 1e3),
+                    "host_link_frac": d2h_s / e2e_s},
             "plain_per_trajectory": {"value": plain_value, "unit": UNIT, "launches_per_step": n_traj,
                                      "ms_per_step": statistics.mean(plain_ms)},
             "batched_vs_plain": value / ws / plain_value,
             "plain_scaling": scaling,
             "entry_points": entries,
+            "single_knot": latency,
             "parity": parity,
             "served": served,
             "served_admission": served_adm,
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                          "frac": achieved_gbs / float(peaks["hbm_gbs"]),
-                         "traffic": (traffic_pk * n) if traffic_pk else None,
+                         "traffic": traffic_pk * n,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel on this "
+                                           "mix (NCU_MIX); the results stay dirty in L2 when the kernel ends",
                          "peak_source": f"{peaks_src} (MEASURED_PEAKS.json hbm_gbs)" if peaks_src == "measured"
                          else "fallback 6.8 TB/s", "bytes_per_knot": BYTES_PER_KNOT,
                          "kernel": "grad_ragged_kernel", "launch_ms": launch_ms},
             "compute_roofline": {"bound": "fp32", "achieved": fp32_achieved, "unit": "TFLOP/s",
-                                 "peak": fp32_peak, "frac": fp32_achieved / fp32_peak,
+                                 "peak": FP32_PEAK_TFLOPS_MEASURED, "frac": fp32_achieved / FP32_PEAK_TFLOPS_MEASURED,
                                  "flop_per_knot": FLOP_PER_KNOT_REF,
-                                 "peak_source": "SMs x 128 FP32 lanes x 2 x sm_max_mhz (nominal)"},
+                                 "executed_flop_per_knot": NCU_MIX["executed_flop_per_knot"],
+                                 "achieved_executed": fp32_executed,
+                                 "frac_executed": fp32_executed / FP32_PEAK_TFLOPS_MEASURED,
+                                 "peak_source": "measured FFMA2 throughput (FP32_PEAK_TFLOPS_MEASURED)"},
             "clocks": dict(clk, window="warm-up (>= 1.5 s of launches) + timed steps"),
             "wall_s_timed_region": wall,
             "gpu_launches": args.steps,

@@ -1,7 +1,7 @@
 """bench.py's contract on CPU: the reference arm's JSON line (the reference
 algorithm's CPU path on this host), its rank handling under torchrun, and the
-helpers the GPU arm's line is built from (the ncu traffic figure read from the
-committed profile, the measured peaks)."""
+helpers the GPU arm's line is built from (the recorded ncu figures of the
+benched kernel, the measured peaks)."""
 import json
 import os
 import subprocess
@@ -48,13 +48,20 @@ def test_reference_arm_other_ranks_do_no_work():
     assert r.stdout.strip() == ""
 
 
-def test_profile_traffic_figure_parses():
-    """The GPU arm's roofline `traffic` is this figure x knots per launch; it must
-    parse and lie between the algorithmic input bytes and twice the algorithmic total."""
+def test_recorded_ncu_figures_are_consistent():
+    """The GPU arm's roofline `traffic` and executed FLOP come from one ncu
+    capture of the benched kernel on the benched mix: DRAM reads cover at least
+    the algorithmic inputs, the executed FP32 work lies below the reference's
+    op count (the kernel drops structural zeros), and the recorded FP32 peak is
+    near the nominal 152 SMs x 128 lanes x 2 x 2.07 GHz."""
     sys.path.insert(0, ROOT)
     import bench
-    t = bench.ncu_traffic_per_knot()
-    assert t is not None and 84 < t < 2 * bench.BYTES_PER_KNOT
+    m = bench.NCU_MIX
+    assert m["knots"] == 66809
+    assert m["dram_read_bytes"] >= 84 * m["knots"]
+    assert 0 < m["executed_flop_per_knot"] < bench.FLOP_PER_KNOT_REF
+    nominal = 152 * 128 * 2 * 2.07e9 / 1e12
+    assert 0.9 * nominal < bench.FP32_PEAK_TFLOPS_MEASURED <= 1.01 * nominal
 
 
 def test_peaks_are_read_from_the_measured_file():
