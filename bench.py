@@ -219,6 +219,23 @@ def plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak, steps=20):
     return out
 
 
+def fp32_peak_live(device):
+    """FP32 CUDA-core peak measured now on `device` by the committed probe
+    frg/bin/frg_fp32_peak (FFMA and packed FFMA2 chains; the larger is the
+    peak); the recorded FP32_PEAK_TFLOPS_MEASURED if the probe cannot run."""
+    exe = os.path.join(ROOT, "fast-rbd-gradients_gb300", "frg", "bin", "frg_fp32_peak")
+    try:
+        r = subprocess.run([exe, str(device), "10"], capture_output=True, text=True, timeout=120)
+        vals = dict(line.split() for line in r.stdout.splitlines() if len(line.split()) == 2)
+        ffma, ffma2 = float(vals["FFMA_TFLOPS"]), float(vals["FFMA2_TFLOPS"])
+        if r.returncode == 0 and ffma > 0:
+            return {"peak": max(ffma, ffma2), "ffma_tflops": ffma, "ffma2_tflops": ffma2,
+                    "source": "measured in this run (frg/bin/frg_fp32_peak: FFMA and FFMA2 chains, best of 10)"}
+    except (OSError, KeyError, ValueError, subprocess.SubprocessError):
+        pass
+    return {"peak": FP32_PEAK_TFLOPS_MEASURED, "source": "recorded FP32_PEAK_TFLOPS_MEASURED (probe unavailable)"}
+
+
 def host_link_rates(torch, dev, stream, nbytes, reps=10):
     """Host link rates (GB/s) of plain copies between pinned host memory and
     device memory, nbytes each, CUDA events on `stream`: the bound of calls
@@ -522,7 +539,8 @@ def run_frg(args):
     link = host_link_rates(torch, dev, stream, 616 * n)
 
     # ---- plain path scaling (one launch per batch of N knots) ----
-    fp32_peak = FP32_PEAK_TFLOPS_MEASURED
+    fp32 = fp32_peak_live(dev.index)
+    fp32_peak = fp32["peak"]
     scaling = plain_scaling(ctx, torch, dev, stream, peaks, fp32_peak)
     entries = entry_points(ctx, torch, dev, stream, peaks)
     latency = single_knot(ctx, torch, dev, stream)
@@ -540,6 +558,7 @@ def run_frg(args):
         achieved_gbs = BYTES_PER_KNOT * n / (launch_ms * 1e-3) / 1e9
         traffic_pk = (NCU_MIX["dram_read_bytes"] + NCU_MIX["dram_write_bytes"]) / NCU_MIX["knots"]
         fp32_achieved = FLOP_PER_KNOT_REF * n / (launch_ms * 1e-3) / 1e12
+        fp32_peak = fp32["peak"]
         fp32_executed = NCU_MIX["executed_flop_per_knot"] * n / (launch_ms * 1e-3) / 1e12
         d2h_s = 616 * n / (link["d2h_gbs"] * 1e9)
         line = {
@@ -578,12 +597,13 @@ def run_frg(args):
                          else "fallback 6.8 TB/s", "bytes_per_knot": BYTES_PER_KNOT,
                          "kernel": "grad_ragged_kernel", "launch_ms": launch_ms},
             "compute_roofline": {"bound": "fp32", "achieved": fp32_achieved, "unit": "TFLOP/s",
-                                 "peak": FP32_PEAK_TFLOPS_MEASURED, "frac": fp32_achieved / FP32_PEAK_TFLOPS_MEASURED,
+                                 "peak": fp32_peak, "frac": fp32_achieved / fp32_peak,
                                  "flop_per_knot": FLOP_PER_KNOT_REF,
                                  "executed_flop_per_knot": NCU_MIX["executed_flop_per_knot"],
                                  "achieved_executed": fp32_executed,
-                                 "frac_executed": fp32_executed / FP32_PEAK_TFLOPS_MEASURED,
-                                 "peak_source": "measured FFMA2 throughput (FP32_PEAK_TFLOPS_MEASURED)"},
+                                 "frac_executed": fp32_executed / fp32_peak,
+                                 "peak_source": fp32["source"],
+                                 "peak_probe": {k: v for k, v in fp32.items() if k.endswith("tflops")}},
             "clocks": dict(clk, window="warm-up (>= 1.5 s of launches) + timed steps"),
             "wall_s_timed_region": wall,
             "gpu_launches": args.steps,

@@ -134,11 +134,22 @@ def build_model(tables, out_dir, verbose=False):
 def build_host_tools(nvcc, force=False, verbose=False):
     """C++ host code over the C ABI, linked to libfrg.so: host/lib<name>.cpp ->
     frg/lib<name>.so (libraries bench.py drives), other host/*.cpp ->
-    frg/bin/<name> (executables)."""
+    frg/bin/<name> (executables); host/*.cu -> frg/bin/<name>, standalone
+    CUDA tools (sm_103a) that do not link libfrg.so."""
     if not os.path.isdir(HOST_SRC):
         return
     os.makedirs(BIN_DIR, exist_ok=True)
     for f in sorted(os.listdir(HOST_SRC)):
+        if f.endswith(".cu"):
+            src, out = os.path.join(HOST_SRC, f), os.path.join(BIN_DIR, f[:-3])
+            if force or _stale(out, [src]):
+                cmd = [nvcc] + ARCH_FLAGS + ["-O3", "-std=c++17", "-lineinfo", src, "-o", out]
+                if verbose:
+                    print(" ".join(cmd), flush=True)
+                r = subprocess.run(cmd, capture_output=True, text=True)
+                if r.returncode != 0:
+                    raise RuntimeError(f"build of {f} failed:\n{r.stdout}\n{r.stderr}")
+            continue
         if not f.endswith(".cpp"):
             continue
         src = os.path.join(HOST_SRC, f)
