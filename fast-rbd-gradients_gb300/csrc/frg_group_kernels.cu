@@ -4,6 +4,7 @@
 // spread over 8x more warps.
 #include "frg_kernels.cuh"
 #include "frg_knot_group.cuh"
+#include "frg_serve.cuh"
 
 namespace frg {
 
@@ -76,12 +77,7 @@ __device__ __forceinline__ void group_persistent(const Seg *segs, int nseg, cons
             const Seg &sg = segs[s];
             const long long i = g - sg.knot_begin;
             if constexpr (SERVE) {
-                const long long h = sg.h;
-                float *hb = sg.host, *db = sg.dev;
-                kp = KnotPtrs{hb + 7 * i, hb + 7 * h + 7 * i, hb + 14 * h + 7 * i, hb + 21 * h + 98 * i,
-                              hb + 119 * h + 7 * i, hb + 126 * h + 49 * i};
-                mr = KnotPtrs{db + 7 * i, db + 7 * h + 7 * i, db + 14 * h + 7 * i, db + 21 * h + 98 * i,
-                              db + 119 * h + 7 * i, db + 126 * h + 49 * i};
+                serve_knot(sg, i, kp, mr);
             } else {
                 kp = KnotPtrs{sg.q + 7 * i, sg.qd + 7 * i, sg.u + 7 * i, sg.dqdd + 98 * i, sg.qdd + 7 * i,
                               sg.minv + 49 * i};

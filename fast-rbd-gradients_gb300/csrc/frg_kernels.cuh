@@ -14,12 +14,17 @@ struct Segment {
     long long knot_begin;
 };
 
-// One server request: a trajectory of h knots whose pinned host slot and
-// device pool slot both hold [q | qd | u | dqdd | qdd | minv] (175 h floats).
-// Inputs are read from the host slot; results go to both slots.
+// One served call: a trajectory of h knots whose device pool slot holds
+// [q | qd | u | dqdd | qdd | minv] (175 h floats).  The call's inputs are read
+// from q, qd, u ([h][7] each): the trajectory's pinned host slot (copied there
+// by submit), its device slot (resident inputs), or the caller's device
+// arrays.  Results always go to the device slot, and also to the pinned host
+// slot (same layout) when host != nullptr.  Inputs read from anywhere but the
+// device slot are mirrored into it, so the next resident call finds them.
 struct ServeSegment {
-    float *host;
+    const float *q, *qd, *u;
     float *dev;
+    float *host;
     long long h;
     long long knot_begin;
 };

@@ -727,11 +727,13 @@ __device__ __forceinline__ void minv_times(real out[7], const real Mi[7][7], con
     }
 }
 
-// Full path for the 32 knots of one warp tile.  With MIRROR, every input and
-// output is also stored at the `mr` pointers (the server keeps a resident
-// device copy of each trajectory while reading inputs from / writing results
-// to its pinned host slot).  With FEXT, kp.fext holds each knot's external
-// link forces; with FDONLY only q̈ and Minv are produced (forward dynamics).
+// Full path for the 32 knots of one warp tile.  With MIRROR, inputs are also
+// stored at mr.q / qd / u and results at mr.dqdd / qdd / minv, for the lanes
+// whose mirror pointers are set (the server mirrors inputs that did not come
+// from a trajectory's device slot into it, and sends results to the pinned
+// host slot when the caller asked for them); a mirror that no lane of the
+// tile wants is skipped.  With FEXT, kp.fext holds each knot's external link
+// forces; with FDONLY only q̈ and Minv are produced (forward dynamics).
 template <bool DAMP, bool MPC, bool MIRROR = false, bool FEXT = false, bool FDONLY = false>
 __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotPtrs &kp,
                                              const KnotPtrs &mr = KnotPtrs{}) {
@@ -747,10 +749,14 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
         u[j] = ws->stage[448 + lane * 7 + j];
     }
     __syncwarp();
+    bool mirror_out = false;
     if constexpr (MIRROR) {
-        scatter_out<7>(ws->stage, const_cast<real *>(mr.q), lane, ws->knot);
-        scatter_out<7>(ws->stage + 224, const_cast<real *>(mr.qd), lane, ws->knot);
-        scatter_out<7>(ws->stage + 448, const_cast<real *>(mr.u), lane, ws->knot);
+        mirror_out = __any_sync(0xffffffffu, mr.minv != nullptr);
+        if (__any_sync(0xffffffffu, mr.q != nullptr)) {
+            scatter_out<7>(ws->stage, const_cast<real *>(mr.q), lane, ws->knot);
+            scatter_out<7>(ws->stage + 224, const_cast<real *>(mr.qd), lane, ws->knot);
+            scatter_out<7>(ws->stage + 448, const_cast<real *>(mr.u), lane, ws->knot);
+        }
     }
     const real *fx = nullptr;
     if constexpr (FEXT) {  // the lane's 42 external-force values stay staged through both RNEA passes
@@ -772,11 +778,11 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
 #pragma unroll
         for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r + 7 * c] = r <= c ? Mi[r][c] : Mi[c][r];
     scatter_out<49>(ws->stage, kp.minv, lane, ws->knot);
-    if constexpr (MIRROR) scatter_out<49>(ws->stage, mr.minv, lane, ws->knot);
+    if (MIRROR && mirror_out) scatter_out<49>(ws->stage, mr.minv, lane, ws->knot);
 #pragma unroll
     for (int r = 0; r < 7; r++) ws->stage[lane * 7 + r] = qdd[r];
     scatter_out<7>(ws->stage, kp.qdd, lane, ws->knot);
-    if constexpr (MIRROR) scatter_out<7>(ws->stage, mr.qdd, lane, ws->knot);
+    if (MIRROR && mirror_out) scatter_out<7>(ws->stage, mr.qdd, lane, ws->knot);
     if constexpr (FDONLY) return;
     if constexpr (!FEXT) {
         rnea_with_qdd<MPC>(ws, lane, qd, qdd, sq, cq);
@@ -806,7 +812,7 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
         }
     }
     scatter_out<49, 98>(ws->stage, kp.dqdd, lane, ws->knot);
-    if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd, lane, ws->knot);
+    if (MIRROR && mirror_out) scatter_out<49, 98>(ws->stage, mr.dqdd, lane, ws->knot);
     // d qdd / dqd: columns 7..13
 #pragma unroll 1
     for (int c = 0; c < kJoints; c += kPair ? 2 : 1) {
@@ -822,7 +828,8 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
         }
     }
     scatter_out<49, 98>(ws->stage, kp.dqdd ? kp.dqdd + 49 : nullptr, lane, ws->knot);
-    if constexpr (MIRROR) scatter_out<49, 98>(ws->stage, mr.dqdd ? mr.dqdd + 49 : nullptr, lane, ws->knot);
+    if (MIRROR && mirror_out)
+        scatter_out<49, 98>(ws->stage, mr.dqdd ? mr.dqdd + 49 : nullptr, lane, ws->knot);
 }
 
 }  // namespace FRG_NS

@@ -374,7 +374,7 @@ __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const Kno
         for (int e = g; e < 49; e += kGroupLanes) kp.minv[e] = gs->minv[ks][e];
         if (g < 7) kp.qdd[g] = gs->qdd[ks][g];
         if constexpr (MIRROR) {
-            if (mr.q) {
+            if (mr.dqdd) {
                 for (int e = g; e < 98; e += kGroupLanes) mr.dqdd[e] = gs->out[ks][e];
                 for (int e = g; e < 49; e += kGroupLanes) mr.minv[e] = gs->minv[ks][e];
                 if (g < 7) mr.qdd[g] = gs->qdd[ks][g];

@@ -1,18 +1,15 @@
-// Server kernel: the batched persistent kernel over server slots.  Inputs
-// come from each request's pinned host slot (read over the host link,
-// coalesced), results are written to the host slot and to the trajectory's
-// resident device pool slot, so a batch needs no per-request copy.
+// Server kernel: the batched persistent kernel over served calls.  Each
+// call's inputs come from where the call has them -- its pinned host slot
+// (read over the host link, coalesced), its resident device slot, or the
+// caller's device arrays -- and its results go to the device slot and, when
+// asked for, to the host slot, so a batch needs no per-call copy.
 #include "frg_kernels.cuh"
 #include "frg_knot.cuh"
+#include "frg_serve.cuh"
 
 namespace frg {
 
 namespace {
-
-__device__ __forceinline__ KnotPtrs slot_knot(float *base, long long h, long long i) {
-    return KnotPtrs{base + 7 * i, base + 7 * h + 7 * i, base + 14 * h + 7 * i, base + 21 * h + 98 * i,
-                    base + 119 * h + 7 * i, base + 126 * h + 49 * i};
-}
 
 template <bool DAMP, bool MPC>
 __global__ void __launch_bounds__(8 * 32)
@@ -34,10 +31,7 @@ __global__ void __launch_bounds__(8 * 32)
         if (g < segs[nseg].knot_begin) {
             int s = tile_seg[ticket];
             while (s + 1 < nseg && segs[s + 1].knot_begin <= g) s++;
-            const ServeSegment &sg = segs[s];
-            const long long i = g - sg.knot_begin;
-            kp = slot_knot(sg.host, sg.h, i);
-            mr = slot_knot(sg.dev, sg.h, i);
+            serve_knot(segs[s], g - segs[s].knot_begin, kp, mr);
         }
         process_tile<DAMP, MPC, true>(ws, lane, kp, mr);
     }

@@ -9,10 +9,16 @@
 //
 // A dispatcher thread folds every ready request into the next batch (up to
 // max_batch_knots knots), uploads the batch's descriptor list with one copy
-// and launches the persistent server kernel, which reads inputs from the
-// pinned host slots and writes results to both slots.  Up to max_inflight
-// batches run at once on their own streams, so requests that arrive while
-// others are on the GPU start without waiting for them.
+// and launches the persistent server kernel.  The kernel reads each call's
+// inputs where the call has them: the pinned host slot (frg_server_submit
+// copies host inputs there), the caller's device arrays
+// (frg_server_submit_device), or the trajectory's device slot
+// (frg_server_submit_resident: the inputs of its previous call, or what the
+// caller wrote there in place).  Inputs from elsewhere are mirrored into the
+// device slot; results go to the device slot, and to the host slot when the
+// caller wants them there.  Up to max_inflight batches run at once on their
+// own streams, so requests that arrive while others are on the GPU start
+// without waiting for them.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -100,15 +106,22 @@ struct Traj {
     int64_t h = 0;
     size_t off = 0, bytes = 0;
     bool admitted = false;
-    bool busy = false;  // a call queued or in flight
+    bool busy = false;             // a call queued or in flight
+    bool inputs_resident = false;  // the device slot holds a complete q, qd, u
 };
 
 enum class ReqState { Admission, Ready, InFlight, Done };
+// Where a call's inputs are: copied to the pinned host slot, the caller's
+// device arrays, or the trajectory's device slot.
+enum class Source { Host, Device, Resident };
 
 struct Request {
     uint64_t id = 0, traj = 0;
     int64_t h = 0;
     ReqState state = ReqState::Admission;
+    Source src = Source::Host;
+    const float *dq = nullptr, *dqd = nullptr, *du = nullptr;  // Source::Device
+    bool host_results = true;
     frg_status status = FRG_OK;
     std::vector<float> staged;  // inputs of a request waiting for admission
     Clock::time_point t_submit, t_launch, t_done;
@@ -183,9 +196,11 @@ void fill_info(const frg_server *s, const Request &r, frg_request_info *info) {
             const Traj &t = it->second;
             const float *hs = s->host_slot(t), *ds = s->dev_slot(t);
             const int64_t h = t.h;
-            info->dqdd = hs + 21 * h;
-            info->qdd = hs + 119 * h;
-            info->minv = hs + 126 * h;
+            if (r.host_results) {
+                info->dqdd = hs + 21 * h;
+                info->qdd = hs + 119 * h;
+                info->minv = hs + 126 * h;
+            }
             info->dev_q = ds;
             info->dev_qd = ds + 7 * h;
             info->dev_u = ds + 14 * h;
@@ -217,7 +232,10 @@ void frg_server::complete_batch(Batch &b, cudaError_t err, Clock::time_point now
         r->t_done = now;
         r->status = err == cudaSuccess ? FRG_OK : FRG_ERR_CUDA;
         auto it = trajs.find(r->traj);
-        if (it != trajs.end()) it->second.busy = false;
+        if (it != trajs.end()) {
+            it->second.busy = false;
+            it->second.inputs_resident = err == cudaSuccess;  // the kernel left this call's inputs in the slot
+        }
         completions.push_back(r->id);
         st.completed++;
         st.knots += static_cast<uint64_t>(r->h);
@@ -256,7 +274,8 @@ void frg_server::run() {
             Request *r = admission.front();
             Traj &t = trajs[r->traj];
             if (!admit(t, r->h)) break;
-            std::memcpy(host_slot(t), r->staged.data(), sizeof(float) * 21 * static_cast<size_t>(r->h));
+            if (r->src == Source::Host)
+                std::memcpy(host_slot(t), r->staged.data(), sizeof(float) * 21 * static_cast<size_t>(r->h));
             r->staged.clear();
             r->staged.shrink_to_fit();
             r->state = ReqState::Ready;
@@ -310,14 +329,26 @@ void frg_server::launch_batch(Batch &b, std::unique_lock<std::mutex> &lk) {
     for (int i = 0; i < nseg; i++) {
         Request *r = b.reqs[i];
         const Traj &t = trajs[r->traj];
-        h_segs[i] = frg::ServeSegment{host_slot(t), dev_slot(t), r->h, begin};
+        float *hs = host_slot(t), *ds = dev_slot(t);
+        const long long h = r->h;
+        const float *q = r->dq, *qd = r->dqd, *u = r->du;  // Source::Device
+        if (r->src == Source::Host) {
+            q = hs;
+            qd = hs + 7 * h;
+            u = hs + 14 * h;
+        } else if (r->src == Source::Resident) {
+            q = ds;
+            qd = ds + 7 * h;
+            u = ds + 14 * h;
+        }
+        h_segs[i] = frg::ServeSegment{q, qd, u, ds, r->host_results ? hs : nullptr, h, begin};
         begin += r->h;
         r->state = ReqState::InFlight;
         r->t_launch = t_launch;
         r->batch = b.id;
         r->batch_requests = nseg;
     }
-    h_segs[nseg] = frg::ServeSegment{nullptr, nullptr, 0, begin};
+    h_segs[nseg] = frg::ServeSegment{nullptr, nullptr, nullptr, nullptr, nullptr, 0, begin};
     const size_t tiles_off = (sizeof(frg::ServeSegment) * (nseg + 1) + 15) / 16 * 16;
     int *h_tiles = reinterpret_cast<int *>(b.h_desc + tiles_off);
     const int ntiles = static_cast<int>((begin + 31) / 32);
@@ -442,61 +473,88 @@ void frg_server_destroy(frg_server *s) {
     delete s;
 }
 
-frg_status frg_server_submit(frg_server *s, uint64_t traj_id, int64_t horizon, const float *q, const float *qd,
-                             const float *u, uint64_t *request_id) {
+}  // extern "C"
+
+namespace {
+
+// One gradient call of trajectory traj_id over `horizon` knots whose inputs
+// are at `src` (host arrays, copied before return; the caller's device arrays;
+// or the trajectory's device slot, horizon ignored).
+frg_status submit_call(frg_server *s, const char *who, uint64_t traj_id, int64_t horizon, Source src,
+                       const float *q, const float *qd, const float *u, bool host_results, uint64_t *request_id) {
     if (!s) return FRG_ERR_INVALID_ARGUMENT;
-    if (horizon <= 0 || !q || !qd || !u) {
-        frg_set_error(s->ctx, "frg_server_submit: horizon must be > 0 and q, qd, u non-null");
+    if (src != Source::Resident && (horizon <= 0 || !q || !qd || !u)) {
+        frg_set_error(s->ctx, std::string(who) + ": horizon must be > 0 and q, qd, u non-null");
         return FRG_ERR_INVALID_ARGUMENT;
     }
-    const size_t bytes = kFloatsPerKnot * sizeof(float) * static_cast<size_t>(horizon);
-    const size_t n7 = 7 * static_cast<size_t>(horizon);
     std::unique_lock<std::mutex> lk(s->mu);
     if (s->stop) return FRG_ERR_SHUTDOWN;
+    if (src == Source::Resident) {
+        auto it = s->trajs.find(traj_id);
+        if (it == s->trajs.end() || !it->second.admitted || !it->second.inputs_resident) {
+            frg_set_error(s->ctx, std::string(who) + ": the trajectory has no resident inputs (no completed call)");
+            return FRG_ERR_NOT_FOUND;
+        }
+        horizon = it->second.h;
+    }
+    const size_t bytes = kFloatsPerKnot * sizeof(float) * static_cast<size_t>(horizon);
+    const size_t n7 = 7 * static_cast<size_t>(horizon);  // floats of one input array
     if (bytes > s->arena.cap()) {
         s->st.rejected++;
-        frg_set_error(s->ctx, "frg_server_submit: horizon " + std::to_string(horizon) +
+        frg_set_error(s->ctx, std::string(who) + ": horizon " + std::to_string(horizon) +
                                   " needs more than the whole device pool");
         return FRG_ERR_ADMISSION;
     }
     if (horizon / 32 + 2 > s->max_tiles_per_batch) {
         s->st.rejected++;
-        frg_set_error(s->ctx, "frg_server_submit: horizon exceeds max_batch_knots");
+        frg_set_error(s->ctx, std::string(who) + ": horizon exceeds max_batch_knots");
         return FRG_ERR_ADMISSION;
     }
     Traj &t = s->trajs[traj_id];
     t.id = traj_id;
     if (t.busy) {
-        frg_set_error(s->ctx, "frg_server_submit: trajectory has a call in flight");
+        frg_set_error(s->ctx, std::string(who) + ": trajectory has a call in flight");
         return FRG_ERR_NOT_READY;
     }
     if (t.admitted && t.h != horizon) {  // horizon changed: new slot
         s->arena.release(t.off, t.bytes);
         t.admitted = false;
+        t.inputs_resident = false;
     }
     auto req = std::make_unique<Request>();
     Request *r = req.get();
     r->id = s->next_req++;
     r->traj = traj_id;
     r->h = horizon;
+    r->src = src;
+    r->host_results = host_results;
+    if (src == Source::Device) {
+        r->dq = q;
+        r->dqd = qd;
+        r->du = u;
+    }
     r->t_submit = Clock::now();
     s->st.submitted++;
     t.busy = true;
     bool admitted = t.admitted || (s->admission.empty() && s->admit(t, horizon));
     if (admitted) {
-        float *slot = s->host_slot(t);
-        lk.unlock();  // the slot belongs to this trajectory and no call of it is in flight
-        std::memcpy(slot, q, sizeof(float) * n7);
-        std::memcpy(slot + n7, qd, sizeof(float) * n7);
-        std::memcpy(slot + 2 * n7, u, sizeof(float) * n7);
-        lk.lock();
+        if (src == Source::Host) {
+            float *slot = s->host_slot(t);
+            lk.unlock();  // the slot belongs to this trajectory and no call of it is in flight
+            std::memcpy(slot, q, sizeof(float) * n7);
+            std::memcpy(slot + n7, qd, sizeof(float) * n7);
+            std::memcpy(slot + 2 * n7, u, sizeof(float) * n7);
+            lk.lock();
+        }
         r->state = ReqState::Ready;
         s->ready.push_back(r);
     } else {
-        r->staged.resize(3 * n7);
-        std::memcpy(r->staged.data(), q, sizeof(float) * n7);
-        std::memcpy(r->staged.data() + n7, qd, sizeof(float) * n7);
-        std::memcpy(r->staged.data() + 2 * n7, u, sizeof(float) * n7);
+        if (src == Source::Host) {
+            r->staged.resize(3 * n7);
+            std::memcpy(r->staged.data(), q, sizeof(float) * n7);
+            std::memcpy(r->staged.data() + n7, qd, sizeof(float) * n7);
+            std::memcpy(r->staged.data() + 2 * n7, u, sizeof(float) * n7);
+        }
         r->state = ReqState::Admission;
         s->admission.push_back(r);
         s->st.admission_stalls++;
@@ -506,6 +564,48 @@ frg_status frg_server_submit(frg_server *s, uint64_t traj_id, int64_t horizon, c
     lk.unlock();
     s->kick.store(true, std::memory_order_release);
     s->cv_dispatch.notify_one();
+    return FRG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+frg_status frg_server_submit(frg_server *s, uint64_t traj_id, int64_t horizon, const float *q, const float *qd,
+                             const float *u, uint64_t *request_id) {
+    return submit_call(s, "frg_server_submit", traj_id, horizon, Source::Host, q, qd, u, true, request_id);
+}
+
+frg_status frg_server_submit_device(frg_server *s, uint64_t traj_id, int64_t horizon, const float *q,
+                                    const float *qd, const float *u, unsigned int flags, uint64_t *request_id) {
+    return submit_call(s, "frg_server_submit_device", traj_id, horizon, Source::Device, q, qd, u,
+                       (flags & FRG_SERVE_HOST_RESULTS) != 0, request_id);
+}
+
+frg_status frg_server_submit_resident(frg_server *s, uint64_t traj_id, unsigned int flags, uint64_t *request_id) {
+    return submit_call(s, "frg_server_submit_resident", traj_id, 0, Source::Resident, nullptr, nullptr, nullptr,
+                       (flags & FRG_SERVE_HOST_RESULTS) != 0, request_id);
+}
+
+frg_status frg_server_slot(frg_server *s, uint64_t traj_id, frg_slot_info *out) {
+    if (!s || !out) return FRG_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->trajs.find(traj_id);
+    if (it == s->trajs.end() || !it->second.admitted || !it->second.inputs_resident) return FRG_ERR_NOT_FOUND;
+    const Traj &t = it->second;
+    if (t.busy) {
+        frg_set_error(s->ctx, "frg_server_slot: trajectory has a call in flight");
+        return FRG_ERR_NOT_READY;
+    }
+    float *ds = s->dev_slot(t);
+    const int64_t h = t.h;
+    out->horizon = h;
+    out->q = ds;
+    out->qd = ds + 7 * h;
+    out->u = ds + 14 * h;
+    out->dqdd = ds + 21 * h;
+    out->qdd = ds + 119 * h;
+    out->minv = ds + 126 * h;
     return FRG_OK;
 }
 

@@ -36,8 +36,9 @@ EXPORTED = (
     "frg_server_wait_any", "frg_server_release", "frg_server_get_stats", "frg_gradient_fext",
     "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64", "frg_get_tuning",
     "frg_set_tuning", "frg_knot_status", "frg_model_name", "frg_gradient_knots", "frg_server_cancel",
-    "frg_single_knot_latency",
+    "frg_single_knot_latency", "frg_server_submit_device", "frg_server_submit_resident", "frg_server_slot",
 )
+SERVE_HOST_RESULTS = 1
 
 KNOT_NONFINITE_INPUT = 1
 KNOT_NONFINITE_OUTPUT = 2
@@ -81,6 +82,11 @@ class RequestInfo(ctypes.Structure):
                 ("dev_qd", ctypes.c_void_p), ("dev_u", ctypes.c_void_p), ("dev_dqdd", ctypes.c_void_p),
                 ("dev_qdd", ctypes.c_void_p), ("dev_minv", ctypes.c_void_p), ("latency_us", ctypes.c_double),
                 ("queue_us", ctypes.c_double), ("batch_id", ctypes.c_uint64), ("batch_requests", ctypes.c_int)]
+
+
+class SlotInfo(ctypes.Structure):
+    _fields_ = [("horizon", ctypes.c_int64), ("q", ctypes.c_void_p), ("qd", ctypes.c_void_p), ("u", ctypes.c_void_p),
+                ("dqdd", ctypes.c_void_p), ("qdd", ctypes.c_void_p), ("minv", ctypes.c_void_p)]
 
 
 class ServerStats(ctypes.Structure):
@@ -141,6 +147,10 @@ def _declare(L):
         "frg_model_name": (ctypes.c_char_p, []),
         "frg_gradient_knots": (st, [vp, i32, vp, vp, vp]),
         "frg_single_knot_latency": (st, [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_double)]),
+        "frg_server_submit_device": (st, [vp, ctypes.c_uint64, i64, vp, vp, vp, ctypes.c_uint,
+                                          ctypes.POINTER(ctypes.c_uint64)]),
+        "frg_server_submit_resident": (st, [vp, ctypes.c_uint64, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint64)]),
+        "frg_server_slot": (st, [vp, ctypes.c_uint64, ctypes.POINTER(SlotInfo)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -429,6 +439,28 @@ class Server:
         st = lib().frg_server_submit(self._h, int(traj_id), int(q.shape[0]), q.ctypes.data, qd.ctypes.data,
                                      u.ctypes.data, ctypes.byref(rid))
         return st, rid.value
+
+    def submit_device(self, traj_id, q, qd, u, host_results=False):
+        """Queue one call on inputs already on the GPU (torch CUDA tensors
+        [h, 7], float32, unchanged until the call completes); returns
+        (status, request_id)."""
+        rid = ctypes.c_uint64()
+        st = lib().frg_server_submit_device(self._h, int(traj_id), int(q.shape[0]), _ptr(q), _ptr(qd), _ptr(u),
+                                            SERVE_HOST_RESULTS if host_results else 0, ctypes.byref(rid))
+        return st, rid.value
+
+    def submit_resident(self, traj_id, host_results=False):
+        """Queue one call on the trajectory's resident device inputs."""
+        rid = ctypes.c_uint64()
+        st = lib().frg_server_submit_resident(self._h, int(traj_id), SERVE_HOST_RESULTS if host_results else 0,
+                                              ctypes.byref(rid))
+        return st, rid.value
+
+    def slot(self, traj_id):
+        """(status, SlotInfo) of the trajectory's device slot."""
+        info = SlotInfo()
+        st = lib().frg_server_slot(self._h, int(traj_id), ctypes.byref(info))
+        return st, info
 
     def wait(self, request_id, timeout_us=-1):
         info = RequestInfo()

@@ -4,7 +4,10 @@ bench_latency():   closed-loop saturation, then Poisson arrivals at 50 % of
                    the saturated session rate: sessions of horizon
                    {16, 32, 64, 128}, 5 calls each, inputs perturbed by
                    N(0, 1e-2) per call; p50/p99 latency overall and for
-                   64-knot calls, throughput.
+                   64-knot calls, throughput.  Once with host inputs and
+                   results (frg_server_submit), once device-resident
+                   (iterates already on the GPU, results kept there:
+                   frg_server_submit_device).
 bench_admission(): 20,000 sessions queued at once, horizons U{8..512}, 10
                    calls each, device pool capped at 2 GiB so admission
                    throttles; throughput, p50/p99, admission stalls, and 1 %
@@ -29,7 +32,7 @@ class LoadgenCfg(ctypes.Structure):
                 ("seed", ctypes.c_uint64), ("sample_frac", ctypes.c_double), ("sample_cap", ctypes.c_int),
                 ("sample_q", ctypes.c_void_p), ("sample_qd", ctypes.c_void_p), ("sample_u", ctypes.c_void_p),
                 ("sample_dqdd", ctypes.c_void_p), ("sample_qdd", ctypes.c_void_p), ("sample_minv", ctypes.c_void_p),
-                ("sample_h", ctypes.c_void_p), ("threads", ctypes.c_int)]
+                ("sample_h", ctypes.c_void_p), ("threads", ctypes.c_int), ("source", ctypes.c_int)]
 
 
 class LoadgenResult(ctypes.Structure):
@@ -56,8 +59,11 @@ def loadgen():
 
 
 def run(server, mode, rate=0.0, concurrency=0, total_sessions=0, duration_s=1.0, calls=5, horizons=(16, 32, 64, 128),
-        horizon_range=None, sigma=1e-2, seed=1, sample_frac=0.0, sample_cap=0, threads=None):
+        horizon_range=None, sigma=1e-2, seed=1, sample_frac=0.0, sample_cap=0, threads=None, source=0):
+    """One load-generator run; source 0: host inputs and results, 1: inputs
+    already on the GPU and results kept there."""
     cfg = LoadgenCfg()
+    cfg.source = int(source)
     cfg.threads = threads or min(8, max(1, (os.cpu_count() or 2) // 2))
     cfg.mode, cfg.rate, cfg.concurrency, cfg.total_sessions = mode, rate, concurrency, total_sessions
     cfg.duration_s, cfg.calls, cfg.sigma, cfg.seed = duration_s, calls, sigma, seed
@@ -92,21 +98,30 @@ def _summ(r, keys):
 
 
 def bench_latency(ctx, seconds=3.0, sat_seconds=1.5, concurrency=512):
-    """Saturation (closed loop) then 50 % load (open loop)."""
-    with Server(ctx, pool_bytes=1 << 30, max_inflight=3) as srv:
-        run(srv, 1, concurrency=64, duration_s=0.3, seed=11)  # warm-up
-        sat = run(srv, 1, concurrency=concurrency, duration_s=sat_seconds, seed=12)
-        session_rate = 0.5 * sat["calls_per_s"] / 5.0
-        half = run(srv, 0, rate=session_rate, duration_s=seconds, seed=13)
-        stats = srv.stats()
+    """Saturation (closed loop) then 50 % load (open loop), for host-submitted
+    calls and for device-resident ones."""
     keys = ("calls", "knots", "sessions", "errors", "elapsed_s", "calls_per_s", "knots_per_s", "p50_us", "p90_us",
             "p99_us", "max_us", "mean_us", "p50_h64_us", "p99_h64_us", "mean_batch_requests")
-    return {
-        "workload": "sessions of horizon {16,32,64,128}, 5 calls each, inputs perturbed by N(0,1e-2) per call",
-        "saturation": dict(_summ(sat, keys), concurrency=concurrency),
-        "half_load": dict(_summ(half, keys), session_rate_per_s=round(session_rate, 1)),
-        "launches": stats["launches"],
-    }
+    out = {"workload": "sessions of horizon {16,32,64,128}, 5 calls each, inputs perturbed by N(0,1e-2) per call"}
+    for source, name in ((0, None), (1, "device_resident")):
+        with Server(ctx, pool_bytes=1 << 30, max_inflight=3) as srv:
+            run(srv, 1, concurrency=64, duration_s=0.3, seed=11, source=source)  # warm-up
+            sat = run(srv, 1, concurrency=concurrency, duration_s=sat_seconds, seed=12, source=source)
+            session_rate = 0.5 * sat["calls_per_s"] / 5.0
+            half = run(srv, 0, rate=session_rate, duration_s=seconds, seed=13, source=source)
+            stats = srv.stats()
+        leg = {
+            "saturation": dict(_summ(sat, keys), concurrency=concurrency),
+            "half_load": dict(_summ(half, keys), session_rate_per_s=round(session_rate, 1)),
+            "launches": stats["launches"],
+        }
+        if name is None:
+            out.update(leg)
+        else:
+            out[name] = dict(leg, calls="frg_server_submit_device: iterates already on the GPU (staged before "
+                                        "the run), results kept in the device slot; latency = submit -> results "
+                                        "in device memory")
+    return out
 
 
 def bench_admission(ctx, sessions=20000, pool_bytes=2 << 30):

@@ -10,7 +10,15 @@
 // `threads` client threads share the session table: each takes the next
 // completion (frg_server_wait_any), perturbs that session's inputs and submits
 // its next call; thread 0 also starts sessions.  Latencies are the server's
-// submit -> results-in-host-memory times.
+// submit -> results-visible times.
+//
+// With `source` 1 the sessions model a solver whose iterates live on the GPU:
+// before the run, kPoolSets sets of `calls` perturbed iterates each are
+// generated and copied to the device in one copy; session s takes set
+// s % kPoolSets (the first h knots of each iterate), each call submits its
+// iterate with frg_server_submit_device, and its results stay in the
+// trajectory's device slot (sampled calls copy them out afterwards).  Starting
+// a session thus makes no CUDA call.
 #include <algorithm>
 #include <atomic>
 #include <mutex>
@@ -22,6 +30,8 @@
 #include <random>
 #include <unordered_map>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "frg.h"
 
@@ -44,6 +54,8 @@ typedef struct frg_loadgen_cfg {
     float *sample_q, *sample_qd, *sample_u, *sample_dqdd, *sample_qdd, *sample_minv;
     int64_t *sample_h;      /* horizon of each sampled call (sample_cap entries) */
     int threads;            /* client threads (>= 1) */
+    int source;             /* 0: host inputs, results to the host (frg_server_submit);
+                               1: device inputs, results kept on the device (frg_server_submit_device) */
 } frg_loadgen_cfg;
 
 typedef struct frg_loadgen_result {
@@ -60,6 +72,8 @@ typedef struct frg_loadgen_result {
 namespace {
 
 using Clock = std::chrono::steady_clock;
+
+constexpr int kPoolSets = 1024;
 
 struct Session {
     uint64_t id;
@@ -90,12 +104,53 @@ extern "C" int frg_loadgen_run(frg_server *srv, const frg_loadgen_cfg *cfg, frg_
     std::atomic<bool> window_open{true};
     int sampled_knots = 0;
     const uint64_t limit = cfg->total_sessions > 0 ? static_cast<uint64_t>(cfg->total_sessions) : UINT64_MAX;
-    const auto t0 = Clock::now();
+    const bool on_device = cfg->source == 1;
+    int max_h = cfg->n_horizons > 0 ? 0 : cfg->horizon_hi;
+    for (int i = 0; i < cfg->n_horizons; i++) max_h = std::max(max_h, cfg->horizons[i]);
+    // source 1: iterate j of set s is [q | qd | u], each 7 * max_h floats, at
+    // (s * calls + j) * 3 * n_max
+    const size_t n_max = 7 * static_cast<size_t>(std::max(max_h, 1));
+    std::vector<float> pool_host;
+    float *pool_dev = nullptr;
+    auto iterate = [&](const float *base, uint64_t sid, int j) {
+        return base + (static_cast<size_t>(sid % kPoolSets) * cfg->calls + j) * 3 * n_max;
+    };
+    if (on_device) {
+        std::mt19937_64 prng(cfg->seed ^ 0x9e3779b97f4a7c15ull);
+        std::uniform_real_distribution<float> unit(-1.0f, 1.0f);
+        std::normal_distribution<float> noise(0.0f, static_cast<float>(cfg->sigma));
+        pool_host.resize(static_cast<size_t>(kPoolSets) * cfg->calls * 3 * n_max);
+        for (int set = 0; set < kPoolSets; set++) {
+            float *it0 = pool_host.data() + static_cast<size_t>(set) * cfg->calls * 3 * n_max;
+            for (size_t i = 0; i < n_max; i++) {
+                it0[i] = lim[i % 7] * unit(prng);
+                it0[n_max + i] = 2.0f * unit(prng);
+                it0[2 * n_max + i] = 20.0f * unit(prng);
+            }
+            for (int j = 1; j < cfg->calls; j++)  // iterate j = iterate j - 1 + N(0, sigma)
+                for (size_t i = 0; i < 3 * n_max; i++)
+                    it0[j * 3 * n_max + i] = it0[(j - 1) * 3 * n_max + i] + noise(prng);
+        }
+        if (cudaMalloc(&pool_dev, sizeof(float) * pool_host.size()) != cudaSuccess ||
+            cudaMemcpy(pool_dev, pool_host.data(), sizeof(float) * pool_host.size(), cudaMemcpyHostToDevice) !=
+                cudaSuccess) {
+            cudaFree(pool_dev);
+            return 1;
+        }
+    }
+    const auto t0 = Clock::now();  // after the staging: the run's clock
     auto elapsed = [&] { return std::chrono::duration<double>(Clock::now() - t0).count(); };
 
     auto submit = [&](Session &s) -> bool {
         uint64_t rid = 0;
-        if (frg_server_submit(srv, s.id, s.h, s.q.data(), s.qd.data(), s.u.data(), &rid) != FRG_OK) {
+        frg_status st;
+        if (on_device) {
+            const float *it = iterate(pool_dev, s.id, s.call);
+            st = frg_server_submit_device(srv, s.id, s.h, it, it + n_max, it + 2 * n_max, 0, &rid);
+        } else {
+            st = frg_server_submit(srv, s.id, s.h, s.q.data(), s.qd.data(), s.u.data(), &rid);
+        }
+        if (st != FRG_OK) {
             errors++;
             return false;
         }
@@ -162,6 +217,7 @@ extern "C" int frg_loadgen_run(frg_server *srv, const frg_loadgen_cfg *cfg, frg_
                 break;
             }
             Session *sp = nullptr;
+            long long dev_sample = -1;  // knot offset of a sampled device-resident call
             {
                 std::lock_guard<std::mutex> lk(mu);
                 auto it = sessions.find(info.traj_id);
@@ -170,15 +226,31 @@ extern "C" int frg_loadgen_run(frg_server *srv, const frg_loadgen_cfg *cfg, frg_
                 if (info.status == FRG_OK && cfg->sample_frac > 0 && u01(rng) < cfg->sample_frac &&
                     sampled_knots + sp->h <= cfg->sample_cap && res->samples < static_cast<uint64_t>(cfg->sample_cap)) {
                     const size_t k0 = static_cast<size_t>(sampled_knots), n = static_cast<size_t>(sp->h);
-                    std::memcpy(cfg->sample_q + 7 * k0, sp->q.data(), 28 * n);
-                    std::memcpy(cfg->sample_qd + 7 * k0, sp->qd.data(), 28 * n);
-                    std::memcpy(cfg->sample_u + 7 * k0, sp->u.data(), 28 * n);
-                    std::memcpy(cfg->sample_dqdd + 98 * k0, info.dqdd, 392 * n);
-                    std::memcpy(cfg->sample_qdd + 7 * k0, info.qdd, 28 * n);
-                    std::memcpy(cfg->sample_minv + 49 * k0, info.minv, 196 * n);
+                    const float *in[3] = {sp->q.data(), sp->qd.data(), sp->u.data()};
+                    if (on_device) {
+                        const float *it = iterate(pool_host.data(), sp->id, sp->call);
+                        in[0] = it;
+                        in[1] = it + n_max;
+                        in[2] = it + 2 * n_max;
+                        dev_sample = static_cast<long long>(k0);
+                    } else {
+                        std::memcpy(cfg->sample_dqdd + 98 * k0, info.dqdd, 392 * n);
+                        std::memcpy(cfg->sample_qdd + 7 * k0, info.qdd, 28 * n);
+                        std::memcpy(cfg->sample_minv + 49 * k0, info.minv, 196 * n);
+                    }
+                    std::memcpy(cfg->sample_q + 7 * k0, in[0], 28 * n);
+                    std::memcpy(cfg->sample_qd + 7 * k0, in[1], 28 * n);
+                    std::memcpy(cfg->sample_u + 7 * k0, in[2], 28 * n);
                     cfg->sample_h[res->samples++] = sp->h;
                     sampled_knots += static_cast<int>(sp->h);
                 }
+            }
+            if (dev_sample >= 0) {  // the call's results are in its device slot until its next call
+                const size_t k0 = static_cast<size_t>(dev_sample), n = static_cast<size_t>(sp->h);
+                if (cudaMemcpy(cfg->sample_dqdd + 98 * k0, info.dev_dqdd, 392 * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                    cudaMemcpy(cfg->sample_qdd + 7 * k0, info.dev_qdd, 28 * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                    cudaMemcpy(cfg->sample_minv + 49 * k0, info.dev_minv, 196 * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+                    errors++;
             }
             Session &s = *sp;  // only this thread touches s until its next call completes
             if (info.status != FRG_OK) errors++;
@@ -189,8 +261,9 @@ extern "C" int frg_loadgen_run(frg_server *srv, const frg_loadgen_cfg *cfg, frg_
             knots += static_cast<uint64_t>(s.h);
             bool finished = ++s.call >= cfg->calls;
             if (!finished) {
-                for (auto *v : {&s.q, &s.qd, &s.u})
-                    for (float &x : *v) x += noise(rng);
+                if (!on_device)
+                    for (auto *v : {&s.q, &s.qd, &s.u})
+                        for (float &x : *v) x += noise(rng);
                 finished = !submit(s);
             }
             if (finished) {
@@ -214,6 +287,7 @@ extern "C" int frg_loadgen_run(frg_server *srv, const frg_loadgen_cfg *cfg, frg_
     client(0);
     for (auto &t : ths) t.join();
 
+    cudaFree(pool_dev);
     res->calls = calls;
     res->knots = knots;
     res->sessions = done_sessions;

@@ -302,7 +302,10 @@ frg_status frg_knot_status(frg_ctx *ctx, int n_knots, const float *q, const floa
  * they arrive:
  *  - a trajectory (traj_id) keeps a slot of 700 B per knot -- its q, qd, u
  *    and its results -- in a capped device pool, mirrored in pinned host
- *    memory, from its first call until frg_server_release;
+ *    memory, from its first call until frg_server_release; a call's inputs
+ *    may come from the host (frg_server_submit), from the caller's device
+ *    arrays (frg_server_submit_device) or from the slot itself
+ *    (frg_server_submit_resident), and its results may stay on the device;
  *  - admission is by free pool bytes: a new trajectory that does not fit
  *    waits (an admission stall) until releases make room;
  *  - a dispatcher thread folds all ready calls into the next persistent
@@ -331,7 +334,8 @@ typedef struct frg_request_info {
     int64_t horizon;
     frg_status status;
     /* results in pinned host memory, valid until this trajectory's next
-     * submit or its release; NULL unless status == FRG_OK */
+     * submit or its release; NULL unless status == FRG_OK and the call wrote
+     * results to the host (frg_server_submit, or FRG_SERVE_HOST_RESULTS) */
     const float *dqdd, *qdd, *minv;
     /* the trajectory's resident device copy (inputs and results) */
     const float *dev_q, *dev_qd, *dev_u, *dev_dqdd, *dev_qdd, *dev_minv;
@@ -361,6 +365,39 @@ void frg_server_destroy(frg_server *srv);
  * never fit the pool. */
 frg_status frg_server_submit(frg_server *srv, uint64_t traj_id, int64_t horizon, const float *q, const float *qd,
                              const float *u, uint64_t *request_id);
+/*
+ * Device-resident calls.  The reference copies every call's inputs and
+ * results across the host link (time_GPU.cu:313-316); these keep a
+ * trajectory's state on the GPU across its solver iterations.
+ *  - frg_server_submit_device: the call's inputs are already on the GPU (a
+ *    solver that computes its next iterate there): q, qd, u [horizon][7] are
+ *    the caller's DEVICE arrays, read by the kernel directly and copied into
+ *    the trajectory's device slot.  They must stay valid and unchanged until
+ *    the call completes.
+ *  - frg_server_submit_resident: a call on the inputs resident in the
+ *    trajectory's device slot -- those of its previous completed call, or what
+ *    the caller wrote there in place through frg_server_slot between calls
+ *    (finished before this submit, e.g. by synchronizing the stream that wrote
+ *    them).  FRG_ERR_NOT_FOUND if the trajectory has no completed call.
+ * Both write results to the device slot (frg_request_info dev_dqdd, dev_qdd,
+ * dev_minv) and, with FRG_SERVE_HOST_RESULTS in flags, to the pinned host
+ * slot as frg_server_submit does.  Admission, batching, errors, cancellation
+ * and determinism are those of frg_server_submit.
+ */
+#define FRG_SERVE_HOST_RESULTS 1u
+frg_status frg_server_submit_device(frg_server *srv, uint64_t traj_id, int64_t horizon, const float *q,
+                                    const float *qd, const float *u, unsigned int flags, uint64_t *request_id);
+frg_status frg_server_submit_resident(frg_server *srv, uint64_t traj_id, unsigned int flags,
+                                      uint64_t *request_id);
+/* The trajectory's device slot: q, qd, u (writable between calls, not while
+ * one is in flight: FRG_ERR_NOT_READY) and the last call's results.
+ * FRG_ERR_NOT_FOUND if the trajectory has no completed call. */
+typedef struct frg_slot_info {
+    int64_t horizon;
+    float *q, *qd, *u;
+    const float *dqdd, *qdd, *minv;
+} frg_slot_info;
+frg_status frg_server_slot(frg_server *srv, uint64_t traj_id, frg_slot_info *out);
 /* FRG_OK (done, info filled, request retired), FRG_ERR_NOT_READY, FRG_ERR_NOT_FOUND. */
 frg_status frg_server_poll(frg_server *srv, uint64_t request_id, frg_request_info *info);
 /* Blocks until the call is done (timeout_us < 0: no limit); FRG_ERR_TIMEOUT otherwise. */
