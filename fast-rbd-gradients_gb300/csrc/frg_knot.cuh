@@ -215,12 +215,23 @@ __device__ __forceinline__ void sts_link(WarpSmem *ws, int k, int lane, const re
     ws->link[kSlotsPerLink * k + 2][lane] = make_real4(Iv[2], Iv[3], Iv[4], Iv[5]);
 }
 
-// sin and cos of a joint angle: the hardware approximation inside [-pi, pi]
-// (absolute error below 2^-21, far inside the 1e-4 parity bar), the
-// range-reducing library routine outside it.
+// sin and cos of a joint angle: the hardware approximation __sincosf
+// (absolute error below 2^-21 on [-pi, pi], far inside the 1e-4 parity bar).
+// An angle outside [-pi, pi] is first reduced by the nearest multiple of 2 pi
+// with Cody and Waite's additive reduction (W. J. Cody, W. Waite, Software
+// Manual for the Elementary Functions, 1980): r = (x - k C1) - k C2 with
+// k = rint(x / 2 pi) and C1 + C2 = 2 pi, C1 = 201/32 short enough that k C1 is
+// exact for |k| < 2^15; each step is one fma, so r is within a few ulp of the
+// true remainder for |x| up to about 10^4 rad.  (The library sincosf's
+// general reduction, never needed for joint angles, cost the kernel a stack
+// frame and 12 % of its time by its code alone.)
 __device__ __forceinline__ void sincos_angle(float x, float *s, float *c) {
-    if (fabsf(x) <= 3.14159f) __sincosf(x, s, c);
-    else sincosf(x, s, c);
+    if (fabsf(x) > 3.14159f) {
+        const float k = rintf(x * 0.159154943f);  // 1 / (2 pi)
+        x = fmaf(-k, 6.28125f, x);                // C1 = 201 / 32
+        x = fmaf(-k, 1.93530718e-3f, x);          // C2 = 2 pi - C1
+    }
+    __sincosf(x, s, c);
 }
 // FP64 verification build: the double-precision library routine throughout.
 __device__ __forceinline__ void sincos_angle(double x, double *s, double *c) { sincos(x, s, c); }

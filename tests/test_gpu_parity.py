@@ -191,14 +191,16 @@ def test_thread_mappings_give_identical_bits(damping, mpc):
 
 
 @pytest.mark.parametrize("lanes", [1, 8])
-def test_angles_beyond_pi_and_large_inputs(lanes):
-    """Joint angles outside [-pi, pi] (up to +-60 rad: the range-reducing sincos
-    path of the FP32 kernels), and velocities and torques ten times the
-    experiment ranges, against the FP64 oracle on the same FP32 inputs."""
+@pytest.mark.parametrize("offsets", [(-60.0, -7.0, -3.5, 3.5, 7.0, 60.0), (-1000.0, -200.0, 200.0, 1000.0)])
+def test_angles_beyond_pi_and_large_inputs(lanes, offsets):
+    """Joint angles outside [-pi, pi] (up to +-1000 rad, a continuous joint
+    after many turns: the range-reduced sincos path of the FP32 kernels), and
+    velocities and torques ten times the experiment ranges, against the FP64
+    oracle on the same FP32 inputs."""
     n = 2048
     q, qd, u = frg.sample_knots(n, seed=314)
     rng = np.random.default_rng(15)
-    q = (q + rng.choice([-60.0, -7.0, -3.5, 3.5, 7.0, 60.0], size=q.shape)).astype(np.float32)
+    q = (q + rng.choice(offsets, size=q.shape)).astype(np.float32)
     qd = (qd * 10).astype(np.float32)
     u = (u * 10).astype(np.float32)
     with frg.Context() as ctx:
