@@ -69,9 +69,10 @@ bool frg_build_batch(int n_traj, const frg_traj *trajs, HostBatch &hb, std::stri
         if (tr.n_knots == 0) continue;
         if (prev) {
             const int64_t m = prev->n_knots;
-            hb.contiguous = tr.q == prev->q + 7 * m && tr.qd == prev->qd + 7 * m && tr.u == prev->u + 7 * m &&
-                            tr.dqdd == prev->dqdd + 98 * m && tr.qdd == prev->qdd + 7 * m &&
-                            tr.minv == prev->minv + 49 * m;
+            using frg::kN;
+            hb.contiguous = tr.q == prev->q + kN * m && tr.qd == prev->qd + kN * m && tr.u == prev->u + kN * m &&
+                            tr.dqdd == prev->dqdd + frg::kDqddN * m && tr.qdd == prev->qdd + kN * m &&
+                            tr.minv == prev->minv + frg::kMinvN * m;
         } else {
             hb.whole = tr;
         }
@@ -158,6 +159,8 @@ void frg_options_default(frg_options *opt) {
 }
 
 const char *frg_model_name(void) { return FRG_MODEL_NAME; }
+
+int frg_model_dofs(void) { return frg::kN; }
 
 const char *frg_status_string(frg_status s) {
     switch (s) {
@@ -425,7 +428,7 @@ frg_status frg_verify_f64(frg_ctx *ctx, int n_knots, const float *q, const float
     }
     if (n_knots == 0) return FRG_OK;
     DeviceGuard g(ctx->device);
-    const size_t n = static_cast<size_t>(n_knots), need = 175 * n;
+    const size_t n = static_cast<size_t>(n_knots), need = frg::kSlotN * n;
     if (ctx->f64_buf_doubles < need) {
         cudaFree(ctx->f64_buf);  // waits for earlier work that may still read it
         ctx->f64_buf = nullptr;
@@ -439,8 +442,8 @@ frg_status frg_verify_f64(frg_ctx *ctx, int n_knots, const float *q, const float
         ctx->f64_buf_doubles = need;
     }
     double *b = ctx->f64_buf;
-    double *q64 = b, *qd64 = b + 7 * n, *u64 = b + 14 * n;
-    double *dqdd64 = b + 21 * n, *qdd64 = b + 119 * n, *minv64 = b + 126 * n;
+    double *q64 = b, *qd64 = b + frg::kSlotQd * n, *u64 = b + frg::kSlotU * n;
+    double *dqdd64 = b + frg::kSlotDqdd * n, *qdd64 = b + frg::kSlotQdd * n, *minv64 = b + frg::kSlotMinv * n;
     if (!check(ctx, frg::launch_widen_inputs(ctx->num_sms, n_knots, q, qd, u, b, stream), "frg_verify_f64 widen") ||
         !check(ctx, frg::launch_plain_f64(ctx->damping, ctx->mpc, ctx->num_sms, n_knots, q64, qd64, u64, dqdd64,
                                           qdd64, minv64, stream),
@@ -486,7 +489,7 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
     // device-to-host rate (about 190 GB/s here) bounds the call.
     if (device_accessible(q) && device_accessible(qd) && device_accessible(u) && device_accessible(dqdd) &&
         device_accessible(qdd) && device_accessible(minv)) {
-        const size_t need = 98 * n;
+        const size_t need = frg::kDqddN * n;
         if (need > ctx->host_buf_floats) {
             cudaFree(ctx->host_buf);
             ctx->host_buf = nullptr;
@@ -507,7 +510,7 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
         return FRG_OK;
     }
     // Pageable host arrays: stage through device buffers owned by ctx.
-    const size_t need = n * (3 * 7 + 98 + 7 + 49);
+    const size_t need = n * frg::kSlotN;
     if (need > ctx->host_buf_floats) {
         cudaFree(ctx->host_buf);
         ctx->host_buf = nullptr;
@@ -519,17 +522,18 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
         }
         ctx->host_buf_floats = need;
     }
-    float *dq = ctx->host_buf, *dqd = dq + 7 * n, *du = dqd + 7 * n, *ddqdd = du + 7 * n, *dqdd_ = ddqdd + 98 * n,
-          *dminv = dqdd_ + 7 * n;
-    const size_t b7 = 7 * n * sizeof(float);
+    float *b = ctx->host_buf;
+    float *dq = b, *dqd = b + frg::kSlotQd * n, *du = b + frg::kSlotU * n, *ddqdd = b + frg::kSlotDqdd * n,
+          *dqdd_ = b + frg::kSlotQdd * n, *dminv = b + frg::kSlotMinv * n;
+    const size_t b7 = frg::kN * n * sizeof(float);
     if (!check(ctx, cudaMemcpyAsync(dq, q, b7, cudaMemcpyHostToDevice, s), "H2D q") ||
         !check(ctx, cudaMemcpyAsync(dqd, qd, b7, cudaMemcpyHostToDevice, s), "H2D qd") ||
         !check(ctx, cudaMemcpyAsync(du, u, b7, cudaMemcpyHostToDevice, s), "H2D u") ||
         !check(ctx, frg::launch_plain(ctx->damping, ctx->mpc, ctx->shape, n_knots, dq, dqd, du, ddqdd, dqdd_, dminv, s),
                "frg_gradient_host launch") ||
-        !check(ctx, cudaMemcpyAsync(dqdd, ddqdd, 98 * n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H dqdd") ||
+        !check(ctx, cudaMemcpyAsync(dqdd, ddqdd, frg::kDqddN * n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H dqdd") ||
         !check(ctx, cudaMemcpyAsync(qdd, dqdd_, b7, cudaMemcpyDeviceToHost, s), "D2H qdd") ||
-        !check(ctx, cudaMemcpyAsync(minv, dminv, 49 * n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H minv") ||
+        !check(ctx, cudaMemcpyAsync(minv, dminv, frg::kMinvN * n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H minv") ||
         !check(ctx, cudaStreamSynchronize(s), "frg_gradient_host sync"))
         return FRG_ERR_CUDA;
     return FRG_OK;
@@ -636,8 +640,8 @@ bool frg_offsets_to_trajs(int n_traj, const int64_t *offsets, const float *q, co
     out.resize(static_cast<size_t>(n_traj));
     for (int t = 0; t < n_traj; t++) {
         const int64_t o = offsets[t];
-        out[t] = frg_traj{offsets[t + 1] - o, q + 7 * o, qd + 7 * o, u + 7 * o, dqdd + 98 * o, qdd + 7 * o,
-                          minv + 49 * o};
+        out[t] = frg_traj{offsets[t + 1] - o, q + frg::kN * o, qd + frg::kN * o, u + frg::kN * o,
+                          dqdd + frg::kDqddN * o, qdd + frg::kN * o, minv + frg::kMinvN * o};
     }
     return true;
 }

@@ -4,11 +4,13 @@
 //   - forward dynamics only: q̈ and Minv (forwardDynamics, :686-706);
 //   - discrete-time Jacobians of one explicit-Euler step from the gradient:
 //       x = [q; qd],  x+ = x + dt [qd; q̈(q, qd, u)]
-//       A = dx+/dx = I + dt [0 I; dq̈/dq dq̈/dqd]   (14 x 14, column-major)
-//       B = dx+/du = dt [0; Minv]                 (14 x 7, column-major)
+//       A = dx+/dx = I + dt [0 I; dq̈/dq dq̈/dqd]   (2N x 2N, column-major)
+//       B = dx+/du = dt [0; Minv]                 (2N x N, column-major)
 //   - the gradient over the reference's packed knot records (knot<T>,
-//     helpers_CPU/dynamicsGradient.h:19-25): [q | qd | u | qdd | Minv], 77
-//     floats per knot, q̈ and Minv written back into the records.
+//     helpers_CPU/dynamicsGradient.h:19-25): [q | qd | u | qdd | Minv],
+//     4N + N^2 floats per knot (77 for 7 joints), q̈ and Minv written back
+//     into the records.
+// N = kN joints (frg_dims.h).
 #include "frg_kernels.cuh"
 #include "frg_knot.cuh"
 
@@ -28,15 +30,15 @@ __global__ void __launch_bounds__(8 * 32)
         const long long g = static_cast<long long>(tile) * 32 + lane;
         KnotPtrs kp{};
         if (g < n) {
-            kp = KnotPtrs{q + 7 * g, qd + 7 * g, u + 7 * g, dqdd ? dqdd + 98 * g : nullptr, qdd + 7 * g,
-                          minv ? minv + 49 * g : nullptr, FEXT ? fext + 42 * g : nullptr};
+            kp = KnotPtrs{q + kN * g, qd + kN * g, u + kN * g, dqdd ? dqdd + kDqddN * g : nullptr, qdd + kN * g,
+                          minv ? minv + kMinvN * g : nullptr, FEXT ? fext + kFextN * g : nullptr};
         }
         process_tile<DAMP, MPC, false, FEXT, FDONLY>(ws, lane, kp);
     }
 }
 
-// Knot records [n][77]: q, qd, u read from each record, q̈ and Minv written
-// into its qdd and Minv fields, the gradient to dqdd [n][98].  The records are
+// Knot records [n][4N + N^2]: q, qd, u read from each record, q̈ and Minv
+// written into its qdd and Minv fields, the gradient to dqdd [n][2N^2].  The records are
 // not tile-contiguous per array, so gather and scatter resolve every knot's
 // address; inputs are staged before any output is written, and the fields do
 // not overlap.
@@ -51,81 +53,84 @@ __global__ void __launch_bounds__(8 * 32) grad_knots_kernel(float *knots, float 
         KnotPtrs kp{};
         if (g < n) {
             float *rec = knots + kKnotRecordFloats * g;
-            kp = KnotPtrs{rec, rec + 7, rec + 14, dqdd + 98 * g, rec + 21, rec + 28};
+            kp = KnotPtrs{rec, rec + kN, rec + 2 * kN, dqdd + kDqddN * g, rec + 3 * kN, rec + 4 * kN};
         }
         process_tile<DAMP, MPC>(ws, lane, kp);
     }
 }
 
-// One thread per output float: A [n][196] then B [n][98].
+// One thread per output float: A [n][4N^2] then B [n][2N^2].
 __global__ void discretize_kernel(int n, const float *dqdd, const float *minv, float dt, float *A, float *B) {
-    const long long total = static_cast<long long>(n) * 294;
+    constexpr int N2 = 2 * kN, NA = N2 * N2, NB = N2 * kN;  // 2N rows; A and B floats per knot
+    const long long total = static_cast<long long>(n) * (NA + NB);
     for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
          e += static_cast<long long>(gridDim.x) * blockDim.x) {
-        if (e < static_cast<long long>(n) * 196) {
-            const long long k = e / 196;
-            const int idx = static_cast<int>(e - k * 196), r = idx % 14, c = idx / 14;
+        if (e < static_cast<long long>(n) * NA) {
+            const long long k = e / NA;
+            const int idx = static_cast<int>(e - k * NA), r = idx % N2, c = idx / N2;
             float v;
-            if (r < 7) v = (c == r + 7) ? dt : 0.0f;  // dq+/dqd = dt I
-            else v = dt * dqdd[98 * k + (r - 7) + 7 * c];
+            if (r < kN) v = (c == r + kN) ? dt : 0.0f;  // dq+/dqd = dt I
+            else v = dt * dqdd[kDqddN * k + (r - kN) + kN * c];
             A[e] = v + (r == c ? 1.0f : 0.0f);
         } else {
-            const long long e2 = e - static_cast<long long>(n) * 196, k = e2 / 98;
-            const int idx = static_cast<int>(e2 - k * 98), r = idx % 14, c = idx / 14;
-            B[e2] = r < 7 ? 0.0f : dt * minv[49 * k + (r - 7) + 7 * c];
+            const long long e2 = e - static_cast<long long>(n) * NA, k = e2 / NB;
+            const int idx = static_cast<int>(e2 - k * NB), r = idx % N2, c = idx / N2;
+            B[e2] = r < kN ? 0.0f : dt * minv[kMinvN * k + (r - kN) + kN * c];
         }
     }
 }
 
 // The same per 64-knot chunk, for 16-byte-aligned arrays.  The chunk's dqdd
-// and Minv (25,088 B and 12,544 B) are staged in shared memory with 16-byte
-// loads; A and B leave as 16-byte stores, coalesced.  Each thread owns one
-// float4 position j of a knot's A (49 float4) and of a knot pair's B (49
-// float4), so the element arithmetic is done once per thread and the loops
-// over the chunk's knots only load, scale and store.  The expressions per
-// element are those of discretize_kernel, so the bits are too.
+// and Minv (25,088 B and 12,544 B for 7 joints) are staged in shared memory
+// with 16-byte loads; A and B leave as 16-byte stores, coalesced.  A knot's A
+// and a knot pair's B are N^2 float4 each (49 for 7 joints); each thread owns
+// one float4 position j of both, so the element arithmetic is done once per
+// thread and the loops over the chunk's knots only load, scale and store.
+// The expressions per element are those of discretize_kernel, so the bits are
+// too.
 constexpr int kDiscKnots = 64;
 __global__ void __launch_bounds__(256) discretize_chunks_kernel(int nchunks, const float *dqdd, const float *minv,
                                                                 float dt, float *A, float *B) {
-    __shared__ float4 s_dqdd4[kDiscKnots * 98 / 4];
-    __shared__ float4 s_minv4[kDiscKnots * 49 / 4];
+    constexpr int N2 = 2 * kN, Q = kN * kN;  // float4 per knot's A and per knot pair's B
+    __shared__ float4 s_dqdd4[kDiscKnots * kDqddN / 4];
+    __shared__ float4 s_minv4[kDiscKnots * kMinvN / 4];
     const float *s_dqdd = reinterpret_cast<const float *>(s_dqdd4);
     const float *s_minv = reinterpret_cast<const float *>(s_minv4);
-    const int ngroups = blockDim.x / 49;  // groups of 49 threads
-    const int g = threadIdx.x / 49, j = threadIdx.x - g * 49;
+    const int ngroups = blockDim.x / Q;  // groups of Q threads
+    const int g = threadIdx.x / Q, j = threadIdx.x - g * Q;
     int asrc[4], bsrc[4];  // offset into the knot's dqdd / the knot pair's Minv, or -1
     float aconst[4], aone[4];
 #pragma unroll
     for (int t = 0; t < 4; t++) {
-        const int idx = 4 * j + t, r = idx % 14, c = idx / 14;  // A element (r, c) of 14 x 14
-        asrc[t] = r < 7 ? -1 : (r - 7) + 7 * c;
-        aconst[t] = r < 7 && c == r + 7 ? dt : 0.0f;
+        const int idx = 4 * j + t, r = idx % N2, c = idx / N2;  // A element (r, c) of 2N x 2N
+        asrc[t] = r < kN ? -1 : (r - kN) + kN * c;
+        aconst[t] = r < kN && c == r + kN ? dt : 0.0f;
         aone[t] = r == c ? 1.0f : 0.0f;
-        const int kp = idx / 98, bi = idx - kp * 98, br = bi % 14, bc = bi / 14;  // B element of knot kp
-        bsrc[t] = br < 7 ? -1 : 49 * kp + (br - 7) + 7 * bc;
+        const int kp = idx / kDqddN, bi = idx - kp * kDqddN, br = bi % N2, bc = bi / N2;  // B element of knot kp
+        bsrc[t] = br < kN ? -1 : kMinvN * kp + (br - kN) + kN * bc;
     }
     for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
         const long long k0 = static_cast<long long>(ch) * kDiscKnots;
-        const float4 *gd = reinterpret_cast<const float4 *>(dqdd + 98 * k0);
-        const float4 *gm = reinterpret_cast<const float4 *>(minv + 49 * k0);
-        for (int i = threadIdx.x; i < kDiscKnots * 98 / 4; i += blockDim.x) s_dqdd4[i] = __ldg(gd + i);
-        for (int i = threadIdx.x; i < kDiscKnots * 49 / 4; i += blockDim.x) s_minv4[i] = __ldg(gm + i);
+        const float4 *gd = reinterpret_cast<const float4 *>(dqdd + kDqddN * k0);
+        const float4 *gm = reinterpret_cast<const float4 *>(minv + kMinvN * k0);
+        for (int i = threadIdx.x; i < kDiscKnots * kDqddN / 4; i += blockDim.x) s_dqdd4[i] = __ldg(gd + i);
+        for (int i = threadIdx.x; i < kDiscKnots * kMinvN / 4; i += blockDim.x) s_minv4[i] = __ldg(gm + i);
         __syncthreads();
         if (g < ngroups) {
-            float4 *gA = reinterpret_cast<float4 *>(A + 196 * k0);
+            float4 *gA = reinterpret_cast<float4 *>(A + 4 * Q * k0);
             for (int kk = g; kk < kDiscKnots; kk += ngroups) {
                 float v[4];
 #pragma unroll
                 for (int t = 0; t < 4; t++)
-                    v[t] = (asrc[t] >= 0 ? dt * s_dqdd[98 * kk + asrc[t]] : aconst[t]) + aone[t];
-                gA[49 * kk + j] = make_float4(v[0], v[1], v[2], v[3]);
+                    v[t] = (asrc[t] >= 0 ? dt * s_dqdd[kDqddN * kk + asrc[t]] : aconst[t]) + aone[t];
+                gA[Q * kk + j] = make_float4(v[0], v[1], v[2], v[3]);
             }
-            float4 *gB = reinterpret_cast<float4 *>(B + 98 * k0);
+            float4 *gB = reinterpret_cast<float4 *>(B + kDqddN * k0);
             for (int kp = g; kp < kDiscKnots / 2; kp += ngroups) {
                 float v[4];
 #pragma unroll
-                for (int t = 0; t < 4; t++) v[t] = bsrc[t] >= 0 ? dt * s_minv[98 * kp + bsrc[t]] : 0.0f;
-                gB[49 * kp + j] = make_float4(v[0], v[1], v[2], v[3]);
+                for (int t = 0; t < 4; t++) v[t] = bsrc[t] >= 0 ? dt * s_minv[kDqddN * kp + bsrc[t]] : 0.0f;
+                gB[Q * kp + j] = make_float4(v[0], v[1], v[2], v[3]);
             }
         }
         __syncthreads();  // the next chunk overwrites the staging
@@ -145,12 +150,12 @@ __device__ __forceinline__ void flag_nonfinite(const float *a, long long n, unsi
 
 __global__ void knot_status_kernel(long long n, const float *q, const float *qd, const float *u, const float *dqdd,
                                    const float *qdd, const float *minv, unsigned int *status) {
-    flag_nonfinite<7>(q, n, 1u, status);
-    flag_nonfinite<7>(qd, n, 1u, status);
-    flag_nonfinite<7>(u, n, 1u, status);
-    flag_nonfinite<98>(dqdd, n, 2u, status);
-    flag_nonfinite<7>(qdd, n, 2u, status);
-    flag_nonfinite<49>(minv, n, 2u, status);
+    flag_nonfinite<kN>(q, n, 1u, status);
+    flag_nonfinite<kN>(qd, n, 1u, status);
+    flag_nonfinite<kN>(u, n, 1u, status);
+    flag_nonfinite<kDqddN>(dqdd, n, 2u, status);
+    flag_nonfinite<kN>(qdd, n, 2u, status);
+    flag_nonfinite<kMinvN>(minv, n, 2u, status);
 }
 
 template <typename K>
@@ -223,11 +228,11 @@ cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float
     const int rest = n - done;
     if (rest > 0) {
         const long long d = done;
-        const long long total = static_cast<long long>(rest) * 294;
+        const long long total = static_cast<long long>(rest) * (6 * kMinvN);
         long long blocks = (total + 255) / 256;
         if (blocks > 152 * 16) blocks = 152 * 16;
-        discretize_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(rest, dqdd + 98 * d, minv + 49 * d, dt,
-                                                                        A + 196 * d, B + 98 * d);
+        discretize_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(rest, dqdd + kDqddN * d, minv + kMinvN * d,
+                                                                        dt, A + 4 * kMinvN * d, B + kDqddN * d);
     }
     return cudaGetLastError();
 }
@@ -251,7 +256,7 @@ cudaError_t launch_knot_status(int num_sms, int n, const float *q, const float *
     if (n <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned int) * static_cast<size_t>(n), stream);
     if (e != cudaSuccess) return e;
-    long long blocks = (static_cast<long long>(n) * 98 + 255) / 256;
+    long long blocks = (static_cast<long long>(n) * kDqddN + 255) / 256;
     if (blocks > static_cast<long long>(num_sms) * 8) blocks = static_cast<long long>(num_sms) * 8;
     knot_status_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(n, q, qd, u, dqdd, qdd, minv, status);
     return cudaGetLastError();

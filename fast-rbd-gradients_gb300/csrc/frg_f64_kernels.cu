@@ -38,15 +38,16 @@ __global__ void __launch_bounds__(32) grad_plain_f64_kernel(Args a) {
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long g = tile * 32 + lane;
         KnotPtrs kp{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-        if (g < a.n) kp = KnotPtrs{a.q + 7 * g, a.qd + 7 * g, a.u + 7 * g, a.dqdd + 98 * g, a.qdd + 7 * g,
-                                   a.minv + 49 * g};
+        if (g < a.n)
+            kp = KnotPtrs{a.q + frg::kN * g, a.qd + frg::kN * g, a.u + frg::kN * g, a.dqdd + frg::kDqddN * g,
+                          a.qdd + frg::kN * g, a.minv + frg::kMinvN * g};
         process_tile<DAMP, MPC>(ws, lane, kp);
     }
 }
 
-// q, qd, u (float, [n][7] each) -> out [3][n][7] (double)
+// q, qd, u (float, [n][N] each) -> out [3][n][N] (double)
 __global__ void widen_inputs_kernel(long long n, const float *q, const float *qd, const float *u, double *out) {
-    const long long m = 7 * n;
+    const long long m = frg::kN * n;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < 3 * m;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
         const long long a = i / m, j = i - a * m;
@@ -73,9 +74,10 @@ __global__ void compare_kernel(long long n, const float *dqdd, const float *qdd,
                                const double *rdqdd, const double *rqdd, const double *rminv, double *err) {
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        err[3 * i + 0] = frob_rel<98>(dqdd + 98 * i, rdqdd + 98 * i);
-        err[3 * i + 1] = frob_rel<7>(qdd + 7 * i, rqdd + 7 * i);
-        err[3 * i + 2] = frob_rel<49>(minv + 49 * i, rminv + 49 * i);
+        constexpr int D = frg::kDqddN, N = frg::kN, M = frg::kMinvN;
+        err[3 * i + 0] = frob_rel<D>(dqdd + D * i, rdqdd + D * i);
+        err[3 * i + 1] = frob_rel<N>(qdd + N * i, rqdd + N * i);
+        err[3 * i + 2] = frob_rel<M>(minv + M * i, rminv + M * i);
     }
 }
 
@@ -135,7 +137,7 @@ cudaError_t launch_plain_f64(bool damping, bool mpc, int num_sms, long long n, c
 cudaError_t launch_widen_inputs(int num_sms, long long n, const float *q, const float *qd, const float *u,
                                 double *out, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
-    frg64::widen_inputs_kernel<<<frg64::stride_grid(num_sms, 21 * n), 256, 0, stream>>>(n, q, qd, u, out);
+    frg64::widen_inputs_kernel<<<frg64::stride_grid(num_sms, 3 * frg::kN * n), 256, 0, stream>>>(n, q, qd, u, out);
     return cudaGetLastError();
 }
 

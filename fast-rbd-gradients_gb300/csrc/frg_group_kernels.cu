@@ -16,7 +16,7 @@ __device__ __forceinline__ KnotPtrs plain_group_knot(const float *q, const float
                                                      float *qdd, float *minv, int n, long long item, int lane) {
     const long long g = item * kGroupKnots + (lane >> 3);
     if (g >= n) return KnotPtrs{};
-    return KnotPtrs{q + 7 * g, qd + 7 * g, u + 7 * g, dqdd + 98 * g, qdd + 7 * g, minv + 49 * g};
+    return KnotPtrs{q + kN * g, qd + kN * g, u + kN * g, dqdd + kDqddN * g, qdd + kN * g, minv + kMinvN * g};
 }
 
 template <bool DAMP, bool MPC>
@@ -45,8 +45,8 @@ __global__ void __launch_bounds__(32)
     GroupSmem *gs = reinterpret_cast<GroupSmem *>(smem_raw);
     for (int i = 0; i < iters; i++) {
         const long long o = static_cast<long long>(i & zero);
-        process_group<DAMP, MPC>(gs, lane, plain_group_knot(q + 7 * o, qd + 7 * o, u + 7 * o, dqdd + 98 * o,
-                                                            qdd + 7 * o, minv + 49 * o, 1, 0, lane));
+        process_group<DAMP, MPC>(gs, lane, plain_group_knot(q + kN * o, qd + kN * o, u + kN * o, dqdd + kDqddN * o,
+                                                            qdd + kN * o, minv + kMinvN * o, 1, 0, lane));
     }
 }
 
@@ -79,8 +79,8 @@ __device__ __forceinline__ void group_persistent(const Seg *segs, int nseg, cons
             if constexpr (SERVE) {
                 serve_knot(sg, i, kp, mr);
             } else {
-                kp = KnotPtrs{sg.q + 7 * i, sg.qd + 7 * i, sg.u + 7 * i, sg.dqdd + 98 * i, sg.qdd + 7 * i,
-                              sg.minv + 49 * i};
+                kp = KnotPtrs{sg.q + kN * i, sg.qd + kN * i, sg.u + kN * i, sg.dqdd + kDqddN * i, sg.qdd + kN * i,
+                              sg.minv + kMinvN * i};
             }
         }
         process_group<DAMP, MPC, SERVE>(gs, lane, kp, mr);

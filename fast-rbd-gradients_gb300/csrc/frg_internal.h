@@ -55,7 +55,7 @@ struct frg_ctx {
     float *host_buf = nullptr;          // device staging for frg_gradient_host (dqdd relay / pageable path)
     size_t host_buf_floats = 0;
     DeviceBatch scratch;                // frg_gradient_batched descriptors
-    double *f64_buf = nullptr;          // frg_verify_f64 scratch (175 doubles per knot)
+    double *f64_buf = nullptr;          // frg_verify_f64 scratch (frg::kSlotN doubles per knot)
     size_t f64_buf_doubles = 0;
     cudaEvent_t scratch_done = nullptr;  // last launch that read `scratch`
 };

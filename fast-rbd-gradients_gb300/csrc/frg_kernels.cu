@@ -12,6 +12,9 @@ namespace frg {
 namespace {
 
 constexpr int kMaxWarpsPerCta = 8;
+// 227 KB of shared memory per CTA: eight warps' staging fits for every
+// supported joint count (28.9 KB per warp at 8 joints, 24.4 KB at 7)
+static_assert(kMaxWarpsPerCta * sizeof(WarpSmem) <= 227 * 1024, "eight warps must fit one CTA");
 
 struct PlainArgs {
     const float *q, *qd, *u;
@@ -23,7 +26,7 @@ struct PlainArgs {
 __device__ __forceinline__ KnotPtrs plain_knot(const PlainArgs &a, int tile, int lane) {
     const long long g = static_cast<long long>(tile) * 32 + lane;
     if (g >= a.n) return KnotPtrs{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    return KnotPtrs{a.q + 7 * g, a.qd + 7 * g, a.u + 7 * g, a.dqdd + 98 * g, a.qdd + 7 * g, a.minv + 49 * g};
+    return KnotPtrs{a.q + kN * g, a.qd + kN * g, a.u + kN * g, a.dqdd + kDqddN * g, a.qdd + kN * g, a.minv + kMinvN * g};
 }
 
 // Floats of `p` that precede it in its 128-byte line.  A warp loop over
@@ -34,24 +37,24 @@ __device__ __forceinline__ int line_shift(const float *p) {
     return static_cast<int>((reinterpret_cast<unsigned long long>(p) & 127ull) / sizeof(float));
 }
 
-// Copies a finished tile's dqdd rows (98 floats per knot, contiguous) from
+// Copies a finished tile's dqdd rows (2N^2 floats per knot, contiguous) from
 // the device array to their final place.  Over the host link only whole
-// aligned lines write at full rate: the two 49-float halves at a 98-float
+// aligned lines write at full rate: the two N^2-float halves at a 2N^2-float
 // stride that process_tile stores run at about 60 % of it, so host results go
 // through device memory (where the tile is still in L2) and leave as one
 // contiguous 12.5 KB run of 16-byte stores.
 __device__ __forceinline__ void relay_dqdd(const PlainArgs &a, int tile, int lane) {
     const long long k0 = static_cast<long long>(tile) * 32;
     const int m = a.n - k0 < 32 ? static_cast<int>(a.n - k0) : 32;
-    const float *src = a.dqdd + 98 * k0;  // written by this warp: plain loads, not the read-only path
-    float *dst = a.dqdd_relay + 98 * k0;
+    const float *src = a.dqdd + kDqddN * k0;  // written by this warp: plain loads, not the read-only path
+    float *dst = a.dqdd_relay + kDqddN * k0;
     if (m == 32 && aligned16(src) && aligned16(dst)) {
         const float4 *s4 = reinterpret_cast<const float4 *>(src);
         float4 *d4 = reinterpret_cast<float4 *>(dst);
 #pragma unroll 5
-        for (int e = lane; e < 98 * 32 / 4; e += 32) d4[e] = s4[e];
+        for (int e = lane; e < kDqddN * 32 / 4; e += 32) d4[e] = s4[e];
     } else {
-        for (int e = lane - line_shift(dst); e < 98 * m; e += 32)
+        for (int e = lane - line_shift(dst); e < kDqddN * m; e += 32)
             if (e >= 0) dst[e] = src[e];
     }
     __syncwarp();
@@ -80,7 +83,7 @@ __device__ __forceinline__ KnotPtrs ragged_knot(const Segment *segs, int nseg, c
     while (s + 1 < nseg && segs[s + 1].knot_begin <= g) s++;
     const Segment &sg = segs[s];
     const long long i = g - sg.knot_begin;
-    return KnotPtrs{sg.q + 7 * i, sg.qd + 7 * i, sg.u + 7 * i, sg.dqdd + 98 * i, sg.qdd + 7 * i, sg.minv + 49 * i};
+    return KnotPtrs{sg.q + kN * i, sg.qd + kN * i, sg.u + kN * i, sg.dqdd + kDqddN * i, sg.qdd + kN * i, sg.minv + kMinvN * i};
 }
 
 // Persistent: each warp takes 32-knot tiles from a device work counter until
@@ -121,8 +124,8 @@ __global__ void __launch_bounds__(32) grad_single_knot_kernel(PlainArgs a, int i
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw);
     for (int i = 0; i < iters; i++) {
         const long long o = static_cast<long long>(i & zero);
-        const KnotPtrs kp = lane == 0 ? KnotPtrs{a.q + 7 * o, a.qd + 7 * o, a.u + 7 * o, a.dqdd + 98 * o,
-                                                 a.qdd + 7 * o, a.minv + 49 * o}
+        const KnotPtrs kp = lane == 0 ? KnotPtrs{a.q + kN * o, a.qd + kN * o, a.u + kN * o, a.dqdd + kDqddN * o,
+                                                 a.qdd + kN * o, a.minv + kMinvN * o}
                                       : KnotPtrs{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
         process_tile<DAMP, MPC>(ws, lane, kp);
     }

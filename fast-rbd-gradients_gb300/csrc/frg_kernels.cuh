@@ -3,10 +3,13 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "frg_dims.h"
+
 namespace frg {
 
 // One trajectory (or any contiguous run of knots) of a ragged batch.  Inputs
-// q/qd/u are [n][7], outputs dqdd [n][98], qdd [n][7], minv [n][49]; knot k
+// q/qd/u are [n][N], outputs dqdd [n][2N^2], qdd [n][N], minv [n][N^2] (N =
+// kN joints, frg_dims.h); knot k
 // of the batch is segment s's knot (k - knot_begin).
 struct Segment {
     const float *q, *qd, *u;
@@ -15,8 +18,8 @@ struct Segment {
 };
 
 // One served call: a trajectory of h knots whose device pool slot holds
-// [q | qd | u | dqdd | qdd | minv] (175 h floats).  The call's inputs are read
-// from q, qd, u ([h][7] each): the trajectory's pinned host slot (copied there
+// [q | qd | u | dqdd | qdd | minv] (kSlotN h floats).  The call's inputs are
+// read from q, qd, u ([h][N] each): the trajectory's pinned host slot (copied there
 // by submit), its device slot (resident inputs), or the caller's device
 // arrays.  Results always go to the device slot, and also to the pinned host
 // slot (same layout) when host != nullptr.  Inputs read from anywhere but the
@@ -51,7 +54,7 @@ cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n
 
 // Plain path for results in host memory (pinned, mapped): q, qd, u, qdd and
 // minv are read and written in place across the host link; dqdd is computed
-// into dqdd_dev (device, [n][98]) and each finished tile is copied to dqdd as
+// into dqdd_dev (device, [n][2N^2]) and each finished tile is copied to dqdd as
 // whole lines.  The latency mapping writes every result in place directly.
 cudaError_t launch_host_out(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
                             const float *u, float *dqdd_dev, float *dqdd, float *qdd, float *minv,
@@ -92,8 +95,8 @@ cudaError_t launch_group_serve(bool damping, bool mpc, const LaunchShape &shape,
                                int nseg, const int *tile_seg, int ntiles, unsigned int *counter, cudaStream_t stream);
 
 // Plain-path variants (frg_ext_kernels.cu): gradient with external forces
-// (fext [n][7][6], link frames), forward dynamics only (fd_only: q̈, optional
-// Minv), and the explicit-Euler discrete Jacobians A [n][196], B [n][98].
+// (fext [n][N][6], link frames), forward dynamics only (fd_only: q̈, optional
+// Minv), and the explicit-Euler discrete Jacobians A [n][4N^2], B [n][2N^2].
 cudaError_t init_ext_kernels();
 cudaError_t launch_ext(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
                        const float *u, const float *fext, float *dqdd, float *qdd, float *minv, bool fd_only,
@@ -101,8 +104,8 @@ cudaError_t launch_ext(bool damping, bool mpc, const LaunchShape &shape, int n, 
 cudaError_t launch_discretize(int n, const float *dqdd, const float *minv, float dt, float *A, float *B,
                               cudaStream_t stream);
 // The reference's packed knot records [n][kKnotRecordFloats]: q, qd, u in;
-// q̈ and Minv written into the records; the gradient to dqdd [n][98].
-constexpr int kKnotRecordFloats = 77;
+// q̈ and Minv written into the records; the gradient to dqdd [n][2N^2].
+constexpr int kKnotRecordFloats = kRecordN;
 cudaError_t launch_knots(bool damping, bool mpc, const LaunchShape &shape, int n, float *knots, float *dqdd,
                          cudaStream_t stream);
 // Per-knot non-finite flags (bit 0 inputs, bit 1 outputs; NULL arrays skipped).
@@ -112,7 +115,7 @@ cudaError_t launch_knot_status(int num_sms, int n, const float *q, const float *
 
 // FP64 verification build (frg_f64_kernels.cu): the plain path in double, and
 // the two helpers of the sampled check of FP32 results (float inputs widened to
-// out [3][n][7]; per-knot Frobenius-relative errors err [n][3] of FP32 dqdd,
+// out [3][n][N]; per-knot Frobenius-relative errors err [n][3] of FP32 dqdd,
 // qdd, minv against FP64 results).
 cudaError_t init_f64_kernels();
 size_t f64_warp_smem_bytes();

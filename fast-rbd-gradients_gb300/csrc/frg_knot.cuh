@@ -23,7 +23,11 @@ namespace FRG_NS {
 //   4: f_k[0,1,3,4] after the backward pass
 constexpr int kSlotsPerLink = 5;
 constexpr int kLinkSlots = kSlotsPerLink * kJoints;
-constexpr int kStageFloats = 49;  // per lane
+// per lane: a knot's dense Minv (N x N) or half of its N x 2N gradient, its
+// 3N inputs, or its 6N external-force values
+constexpr int kStageFloats = kJoints * kJoints > 6 * kJoints ? kJoints * kJoints : 6 * kJoints;
+constexpr int kMinvFloats = kJoints * kJoints;
+constexpr int kDqddFloats = 2 * kJoints * kJoints;
 
 // Four reals as one 16-byte-aligned shared-memory slot.
 template <typename T> struct Real4Of;
@@ -56,7 +60,7 @@ struct WarpSmem {
 struct KnotPtrs {
     const real *q, *qd, *u;
     real *dqdd, *qdd, *minv;
-    const real *fext = nullptr;  // [7][6] external spatial force per link (link frame), optional
+    const real *fext = nullptr;  // [kJoints][6] external spatial force per link (link frame), optional
 };
 
 __device__ __forceinline__ const real *shfl_ptr(const real *p, int src) {
@@ -118,7 +122,7 @@ __device__ __forceinline__ void gather_in(real *stage, const real *base, int lan
         for (int e = lane; e < 32 * W; e += 32) stage[e] = e < lim ? __ldg(b0 + e) : real(0);
         return;
     }
-    if constexpr (W <= 7) {
+    if constexpr (W <= 8) {
         knot[lane] = base;
         __syncwarp();
         int kn = lane / W, j = lane % W;
@@ -149,7 +153,7 @@ __device__ __forceinline__ void gather_in(real *stage, const real *base, int lan
 // a few cache lines.  A lane storing only its own knot would turn every store
 // instruction into 32 separate cache-line writes; with many such tiles in
 // flight the L2 request rate, not the arithmetic, then sets the time.  The
-// stores go in groups of 7 after the group's table and stage reads: the
+// stores go in groups of kJoints after the group's table and stage reads: the
 // compiler cannot tell a table pointer from shared memory, so a read placed
 // after a store would wait for it.
 template <int W, int STRIDE = W>
@@ -179,23 +183,24 @@ __device__ __forceinline__ void scatter_out(const real *stage, real *base, int l
             }
         }
     } else {
-        static_assert(W % 7 == 0, "split-tile stores go in groups of 7");
+        constexpr int G = kJoints;  // every W here is a multiple of the joint count
+        static_assert(W % G == 0, "split-tile stores go in groups of kJoints");
         knot[lane] = base;
         __syncwarp();
         int kn = lane / W, j = lane % W;
 #pragma unroll 1
-        for (int m0 = 0; m0 < W; m0 += 7) {
-            real *p[7];
-            real v[7];
+        for (int m0 = 0; m0 < W; m0 += G) {
+            real *p[G];
+            real v[G];
 #pragma unroll
-            for (int i = 0; i < 7; i++) {
+            for (int i = 0; i < G; i++) {
                 p[i] = const_cast<real *>(knot[kn]);
                 if (p[i]) p[i] += j;
                 v[i] = stage[lane + 32 * (m0 + i)];
                 next_element<W>(kn, j);
             }
 #pragma unroll
-            for (int i = 0; i < 7; i++)
+            for (int i = 0; i < G; i++)
                 if (p[i]) *p[i] = v[i];
         }
     }
@@ -391,8 +396,9 @@ __device__ __forceinline__ void add_link_inertia(real A[3][3], real B[3][3], rea
 // sincos, RNEA(q, qd, 0), bias, Minv (upper triangle, Mi[i][j] for i <= j), qdd.
 // Leaves v_k and I_k v_k of every link in the warp's link slots.
 template <bool DAMP, bool MPC, bool FEXT = false>
-__device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const real q[7], const real qd[7], const real u[7],
-                                       real sq[7], real cq[7], real Mi[7][7], real qdd[7],
+__device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const real q[kJoints], const real qd[kJoints],
+                                       const real u[kJoints], real sq[kJoints], real cq[kJoints],
+                                       real Mi[kJoints][kJoints], real qdd[kJoints],
                                        const real *fx = nullptr) {
 #pragma unroll
     for (int k = 0; k < kJoints; k++) sincos_angle(q[k], &sq[k], &cq[k]);
@@ -542,8 +548,9 @@ __device__ __forceinline__ void phase1(WarpSmem *ws, int lane, const real q[7], 
 // accumulated f_k[0,1,3,4] in the link slots (read at the diagonal step of the
 // d/dq sweeps).
 template <bool MPC, bool FEXT = false>
-__device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const real qd[7], const real qdd[7],
-                                              const real sq[7], const real cq[7], const real *fx = nullptr) {
+__device__ __forceinline__ void rnea_with_qdd(WarpSmem *ws, int lane, const real qd[kJoints],
+                                              const real qdd[kJoints], const real sq[kJoints], const real cq[kJoints],
+                                              const real *fx = nullptr) {
     real f[kJoints][6];
     real a[6];
     static_for<0, kJoints>([&](auto K) {
@@ -654,8 +661,9 @@ __device__ __forceinline__ void advance_column(real dv[6], real da[6], real qdk,
 // k - 1 with the velocity / acceleration tangents of link k.  The link loop is
 // unrolled; c is a warp-uniform runtime value.
 template <bool QSIDE, bool DAMP, bool PAIR>
-__device__ __forceinline__ void dtau_column_pair(const WarpSmem *ws, int lane, int c, const real qd[7],
-                                                 const real sq[7], const real cq[7], real dtA[7], real dtB[7]) {
+__device__ __forceinline__ void dtau_column_pair(const WarpSmem *ws, int lane, int c, const real qd[kJoints],
+                                                 const real sq[kJoints], const real cq[kJoints], real dtA[kJoints],
+                                                 real dtB[kJoints]) {
     const int cb = PAIR ? c + 1 : kJoints;
     real dfA[kJoints][6], dfB[kJoints][6];
     real dvA[6], daA[6], dvB[6], daB[6];
@@ -728,7 +736,8 @@ __device__ __forceinline__ void dtau_column_pair(const WarpSmem *ws, int lane, i
 }
 
 // out = -Minv_sym dtau
-__device__ __forceinline__ void minv_times(real out[7], const real Mi[7][7], const real dtau[7]) {
+__device__ __forceinline__ void minv_times(real out[kJoints], const real Mi[kJoints][kJoints],
+                                           const real dtau[kJoints]) {
 #pragma unroll
     for (int r = 0; r < kJoints; r++) {
         real acc = 0.0f;
@@ -748,35 +757,37 @@ __device__ __forceinline__ void minv_times(real out[7], const real Mi[7][7], con
 template <bool DAMP, bool MPC, bool MIRROR = false, bool FEXT = false, bool FDONLY = false>
 __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotPtrs &kp,
                                              const KnotPtrs &mr = KnotPtrs{}) {
-    real q[7], qd[7], u[7];
-    gather_in<7>(ws->stage, kp.q, lane, ws->knot);
-    gather_in<7>(ws->stage + 224, kp.qd, lane, ws->knot);
-    gather_in<7>(ws->stage + 448, kp.u, lane, ws->knot);
+    constexpr int N = kJoints, NN = kMinvFloats;
+    real *const st_q = ws->stage, *const st_qd = ws->stage + 32 * N, *const st_u = ws->stage + 64 * N;
+    real q[N], qd[N], u[N];
+    gather_in<N>(st_q, kp.q, lane, ws->knot);
+    gather_in<N>(st_qd, kp.qd, lane, ws->knot);
+    gather_in<N>(st_u, kp.u, lane, ws->knot);
     __syncwarp();
 #pragma unroll
-    for (int j = 0; j < 7; j++) {
-        q[j] = ws->stage[lane * 7 + j];
-        qd[j] = ws->stage[224 + lane * 7 + j];
-        u[j] = ws->stage[448 + lane * 7 + j];
+    for (int j = 0; j < N; j++) {
+        q[j] = st_q[lane * N + j];
+        qd[j] = st_qd[lane * N + j];
+        u[j] = st_u[lane * N + j];
     }
     __syncwarp();
     bool mirror_out = false;
     if constexpr (MIRROR) {
         mirror_out = __any_sync(0xffffffffu, mr.minv != nullptr);
         if (__any_sync(0xffffffffu, mr.q != nullptr)) {
-            scatter_out<7>(ws->stage, const_cast<real *>(mr.q), lane, ws->knot);
-            scatter_out<7>(ws->stage + 224, const_cast<real *>(mr.qd), lane, ws->knot);
-            scatter_out<7>(ws->stage + 448, const_cast<real *>(mr.u), lane, ws->knot);
+            scatter_out<N>(st_q, const_cast<real *>(mr.q), lane, ws->knot);
+            scatter_out<N>(st_qd, const_cast<real *>(mr.qd), lane, ws->knot);
+            scatter_out<N>(st_u, const_cast<real *>(mr.u), lane, ws->knot);
         }
     }
     const real *fx = nullptr;
-    if constexpr (FEXT) {  // the lane's 42 external-force values stay staged through both RNEA passes
-        gather_in<42>(ws->stage, kp.fext, lane, ws->knot);
+    if constexpr (FEXT) {  // the lane's 6N external-force values stay staged through both RNEA passes
+        gather_in<6 * N>(ws->stage, kp.fext, lane, ws->knot);
         __syncwarp();
-        fx = ws->stage + lane * 42;
+        fx = ws->stage + lane * 6 * N;
     }
 
-    real sq[7], cq[7], Mi[7][7], qdd[7];
+    real sq[N], cq[N], Mi[N][N], qdd[N];
     phase1<DAMP, MPC, FEXT>(ws, lane, q, qd, u, sq, cq, Mi, qdd, fx);
     // with FEXT the second RNEA runs while the forces are still staged;
     // otherwise after the Minv / qdd stores (fewer live registers)
@@ -785,62 +796,62 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
 
     // Minv (dense) and qdd out
 #pragma unroll
-    for (int c = 0; c < 7; c++)
+    for (int c = 0; c < N; c++)
 #pragma unroll
-        for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r + 7 * c] = r <= c ? Mi[r][c] : Mi[c][r];
-    scatter_out<49>(ws->stage, kp.minv, lane, ws->knot);
-    if (MIRROR && mirror_out) scatter_out<49>(ws->stage, mr.minv, lane, ws->knot);
+        for (int r = 0; r < N; r++) ws->stage[lane * NN + r + N * c] = r <= c ? Mi[r][c] : Mi[c][r];
+    scatter_out<NN>(ws->stage, kp.minv, lane, ws->knot);
+    if (MIRROR && mirror_out) scatter_out<NN>(ws->stage, mr.minv, lane, ws->knot);
 #pragma unroll
-    for (int r = 0; r < 7; r++) ws->stage[lane * 7 + r] = qdd[r];
-    scatter_out<7>(ws->stage, kp.qdd, lane, ws->knot);
-    if (MIRROR && mirror_out) scatter_out<7>(ws->stage, mr.qdd, lane, ws->knot);
+    for (int r = 0; r < N; r++) ws->stage[lane * N + r] = qdd[r];
+    scatter_out<N>(ws->stage, kp.qdd, lane, ws->knot);
+    if (MIRROR && mirror_out) scatter_out<N>(ws->stage, mr.qdd, lane, ws->knot);
     if constexpr (FDONLY) return;
     if constexpr (!FEXT) {
         rnea_with_qdd<MPC>(ws, lane, qd, qdd, sq, cq);
         __syncwarp();
     }
 
-    // d qdd / dq: columns 0..6 (column 0 is identically zero when the base
+    // d qdd / dq: columns 0..N-1 (column 0 is identically zero when the base
     // joint axis is parallel to gravity, as for the iiwa and as
     // dynamicsGradient.h:797-813 uses; other models compute it)
     if constexpr (kDqColumn0Zero) {
 #pragma unroll
-        for (int r = 0; r < 7; r++) ws->stage[lane * 49 + r] = 0.0f;
+        for (int r = 0; r < N; r++) ws->stage[lane * NN + r] = 0.0f;
     }
     // two columns per sweep; one with FEXT, whose staged forces leave fewer registers
     constexpr bool kPair = !FEXT;
 #pragma unroll 1
-    for (int c = kDqColumn0Zero ? 1 : 0; c < kJoints; c += kPair ? 2 : 1) {
-        real dtA[7], dtB[7], out[7];
+    for (int c = kDqColumn0Zero ? 1 : 0; c < N; c += kPair ? 2 : 1) {
+        real dtA[N], dtB[N], out[N];
         dtau_column_pair<true, DAMP, kPair>(ws, lane, c, qd, sq, cq, dtA, dtB);
         minv_times(out, Mi, dtA);
 #pragma unroll
-        for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
-        if (kPair && c + 1 < kJoints) {
+        for (int r = 0; r < N; r++) ws->stage[lane * NN + N * c + r] = out[r];
+        if (kPair && c + 1 < N) {
             minv_times(out, Mi, dtB);
 #pragma unroll
-            for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * (c + 1) + r] = out[r];
+            for (int r = 0; r < N; r++) ws->stage[lane * NN + N * (c + 1) + r] = out[r];
         }
     }
-    scatter_out<49, 98>(ws->stage, kp.dqdd, lane, ws->knot);
-    if (MIRROR && mirror_out) scatter_out<49, 98>(ws->stage, mr.dqdd, lane, ws->knot);
-    // d qdd / dqd: columns 7..13
+    scatter_out<NN, 2 * NN>(ws->stage, kp.dqdd, lane, ws->knot);
+    if (MIRROR && mirror_out) scatter_out<NN, 2 * NN>(ws->stage, mr.dqdd, lane, ws->knot);
+    // d qdd / dqd: columns N..2N-1
 #pragma unroll 1
-    for (int c = 0; c < kJoints; c += kPair ? 2 : 1) {
-        real dtA[7], dtB[7], out[7];
+    for (int c = 0; c < N; c += kPair ? 2 : 1) {
+        real dtA[N], dtB[N], out[N];
         dtau_column_pair<false, DAMP, kPair>(ws, lane, c, qd, sq, cq, dtA, dtB);
         minv_times(out, Mi, dtA);
 #pragma unroll
-        for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * c + r] = out[r];
-        if (kPair && c + 1 < kJoints) {
+        for (int r = 0; r < N; r++) ws->stage[lane * NN + N * c + r] = out[r];
+        if (kPair && c + 1 < N) {
             minv_times(out, Mi, dtB);
 #pragma unroll
-            for (int r = 0; r < 7; r++) ws->stage[lane * 49 + 7 * (c + 1) + r] = out[r];
+            for (int r = 0; r < N; r++) ws->stage[lane * NN + N * (c + 1) + r] = out[r];
         }
     }
-    scatter_out<49, 98>(ws->stage, kp.dqdd ? kp.dqdd + 49 : nullptr, lane, ws->knot);
+    scatter_out<NN, 2 * NN>(ws->stage, kp.dqdd ? kp.dqdd + NN : nullptr, lane, ws->knot);
     if (MIRROR && mirror_out)
-        scatter_out<49, 98>(ws->stage, mr.dqdd ? mr.dqdd + 49 : nullptr, lane, ws->knot);
+        scatter_out<NN, 2 * NN>(ws->stage, mr.dqdd ? mr.dqdd + NN : nullptr, lane, ws->knot);
 }
 
 }  // namespace FRG_NS

@@ -6,9 +6,11 @@
 // group share a knot:
 //   - phase 1 (sincos, RNEA, articulated inertias, q̈) runs replicated in all
 //     8 lanes, except the Minv column passes: lane g computes column g;
-//   - the 13 non-zero dtau columns are split so that every lane walks 7 link
-//     steps: lane g takes dtau/dqd column g and dtau/dq column 7 - g;
-//   - lane g then writes output columns g and 7 + (7 - g) of -Minv dtau.
+//   - the dtau columns are split so that every lane walks about N link steps
+//     (N joints, at most 8): lane g takes dtau/dqd column g and dtau/dq
+//     column N - g (dtau/dq column 0, where the model needs it, on lane N, or
+//     on lane 0 for N = 8), which for the 7-joint iiwa gives every lane 7;
+//   - each lane then writes its output columns of -Minv dtau.
 // Lane-dependent work is predicated (selects), so a group never diverges.
 // About 2.5x less latency per knot than the knot-per-lane mapping, at about
 // 3x its instructions per knot: the autotuner and the server pick by size.
@@ -20,12 +22,22 @@ namespace frg {
 constexpr int kGroupLanes = 8;
 constexpr int kGroupKnots = 32 / kGroupLanes;  // knots per warp
 
+static_assert(kJoints <= kGroupLanes, "one lane per joint column");
+
 struct GroupSmem {
     float4 link[kGroupKnots][kLinkSlots];  // per knot, slot layout as WarpSmem
-    float minv[kGroupKnots][49];           // dense Minv
-    float out[kGroupKnots][98];            // dqdd staging
+    float minv[kGroupKnots][kMinvN];       // dense Minv
+    float out[kGroupKnots][kDqddN];        // dqdd staging
     float qdd[kGroupKnots][8];
 };
+
+// The dtau/dq column of group lane g (kJoints: none): column N - g for
+// g = 1..N-1, column 0 on lane N (lane 0 when N = 8, the only free lane).
+__device__ __forceinline__ int g_q_column(int g) {
+    if (g >= 1 && g < kJoints) return kJoints - g;
+    const int lane0 = kJoints < kGroupLanes ? kJoints : 0;
+    return (g == lane0 && !kDqColumn0Zero) ? 0 : kJoints;
+}
 
 template <int k> __device__ __forceinline__ void g_sts(GroupSmem *gs, int ks, int slot, float4 v) {
     gs->link[ks][kSlotsPerLink * k + slot] = v;
@@ -39,12 +51,13 @@ __device__ __forceinline__ void g_lds_link(const GroupSmem *gs, int ks, int k, f
     Iv[0] = b.z; Iv[1] = b.w; Iv[2] = c.x; Iv[3] = c.y; Iv[4] = c.z; Iv[5] = c.w;
 }
 
-// One dtau column per lane, lane-dependent c (0..7; c == 7: no column).
+// One dtau column per lane, lane-dependent c (0..N-1; c == N: no column).
 // Same recursions as dtau_column in frg_knot.cuh, with the k >= c / k == c
 // choices made by selects so that the 8 lanes of a group stay converged.
 template <bool QSIDE, bool DAMP>
-__device__ __forceinline__ void g_dtau_column(const GroupSmem *gs, int ks, int c, const float qd[7],
-                                              const float sq[7], const float cq[7], float dtau[7]) {
+__device__ __forceinline__ void g_dtau_column(const GroupSmem *gs, int ks, int c, const float qd[kJoints],
+                                              const float sq[kJoints], const float cq[kJoints],
+                                              float dtau[kJoints]) {
     float df[kJoints][6];
     float dv[6] = {0, 0, 0, 0, 0, 0}, da[6] = {0, 0, 0, 0, 0, 0};
     static_for<0, kJoints>([&](auto K) {
@@ -120,19 +133,20 @@ __device__ __forceinline__ void g_dtau_column(const GroupSmem *gs, int ks, int c
 template <bool DAMP, bool MPC, bool MIRROR = false>
 __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const KnotPtrs &kp,
                                               const KnotPtrs &mr = KnotPtrs{}) {
+    constexpr int N = kJoints, NN = kMinvN;
     const int ks = lane >> 3, g = lane & 7;
-    float q[7], qd[7], u[7];
+    float q[N], qd[N], u[N];
 #pragma unroll
-    for (int j = 0; j < 7; j++) {
+    for (int j = 0; j < N; j++) {
         q[j] = kp.q ? __ldg(kp.q + j) : 0.0f;
         qd[j] = kp.q ? __ldg(kp.qd + j) : 0.0f;
         u[j] = kp.q ? __ldg(kp.u + j) : 0.0f;
     }
     if constexpr (MIRROR) {
-        if (mr.q && g < 7) {  // entry g, picked with compile-time indices (no local-memory arrays)
+        if (mr.q && g < N) {  // entry g, picked with compile-time indices (no local-memory arrays)
             float qg = q[0], qdg = qd[0], ug = u[0];
 #pragma unroll
-            for (int j = 1; j < 7; j++) {
+            for (int j = 1; j < N; j++) {
                 if (j == g) {
                     qg = q[j];
                     qdg = qd[j];
@@ -144,7 +158,7 @@ __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const Kno
             const_cast<float *>(mr.u)[g] = ug;
         }
     }
-    float sq[7], cq[7];
+    float sq[N], cq[N];
 #pragma unroll
     for (int k = 0; k < kJoints; k++) sincos_angle(q[k], &sq[k], &cq[k]);
 
@@ -228,10 +242,11 @@ __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const Kno
         });
     }
 
-    // Minv column j = g (lane 7 repeats column 6): backward then forward pass
-    // with the rows i > j masked to zero (minv.h:392-469 restricted to column j)
+    // Minv column j = g (lanes g >= N repeat column N - 1): backward then
+    // forward pass with the rows i > j masked to zero (minv.h:392-469
+    // restricted to column j)
     {
-        const int j = g < 7 ? g : 6;
+        const int j = g < N ? g : N - 1;
         float col[kJoints];
         float F[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         static_for_down<kJoints - 1, 0>([&](auto II) {
@@ -265,25 +280,25 @@ __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const Kno
                 F[2] += col[i];
             }
         });
-        if (g < 7) {
+        if (g < N) {
 #pragma unroll
             for (int i = 0; i < kJoints; i++)
                 if (i <= j) {
-                    gs->minv[ks][i + 7 * j] = col[i];
-                    gs->minv[ks][j + 7 * i] = col[i];
+                    gs->minv[ks][i + N * j] = col[i];
+                    gs->minv[ks][j + N * i] = col[i];
                 }
         }
     }
     __syncwarp();
-    // qdd = Minv bias (lane g < 7 computes entry g, shares it through smem)
-    if (g < 7) {
+    // qdd = Minv bias (lane g < N computes entry g, shares it through smem)
+    if (g < N) {
         float acc = 0.0f;
 #pragma unroll
-        for (int k = 0; k < kJoints; k++) acc = fmaf(gs->minv[ks][g + 7 * k], bias[k], acc);
+        for (int k = 0; k < kJoints; k++) acc = fmaf(gs->minv[ks][g + N * k], bias[k], acc);
         gs->qdd[ks][g] = acc;
     }
     __syncwarp();
-    float qdd[7];
+    float qdd[N];
 #pragma unroll
     for (int k = 0; k < kJoints; k++) qdd[k] = gs->qdd[ks][k];
 
@@ -330,54 +345,53 @@ __device__ __forceinline__ void process_group(GroupSmem *gs, int lane, const Kno
     }
     __syncwarp();
 
-    // tangent columns: dqd column g and dq column 7 - g (none for g = 7 / 0;
-    // lane 7's dq column 0 is computed unless the model makes it vanish)
-    float mrow[7][7];
+    // tangent columns: dqd column g (lanes g < N) and dq column g_q_column(g)
+    float mrow[N][N];
 #pragma unroll
-    for (int r = 0; r < 7; r++)
+    for (int r = 0; r < N; r++)
 #pragma unroll
-        for (int k = 0; k < 7; k++) mrow[r][k] = gs->minv[ks][r + 7 * k];
+        for (int k = 0; k < N; k++) mrow[r][k] = gs->minv[ks][r + N * k];
     {
-        float dtau[7];
-        g_dtau_column<false, DAMP>(gs, ks, g, qd, sq, cq, dtau);  // g = 7: all-zero column, unused
-        if (g < 7) {
+        float dtau[N];
+        g_dtau_column<false, DAMP>(gs, ks, g < N ? g : N, qd, sq, cq, dtau);  // c = N: all-zero column, unused
+        if (g < N) {
 #pragma unroll
-            for (int r = 0; r < 7; r++) {
+            for (int r = 0; r < N; r++) {
                 float acc = 0.0f;
 #pragma unroll
-                for (int k = 0; k < 7; k++) acc = fmaf(mrow[r][k], dtau[k], acc);
-                gs->out[ks][49 + 7 * g + r] = -acc;
+                for (int k = 0; k < N; k++) acc = fmaf(mrow[r][k], dtau[k], acc);
+                gs->out[ks][NN + N * g + r] = -acc;
             }
         }
     }
     {
-        const int cq_col = 7 - g;  // 7 (g = 0): no column
-        float dtau[7];
+        const int cq_col = g_q_column(g);  // N: no column
+        float dtau[N];
         g_dtau_column<true, DAMP>(gs, ks, cq_col, qd, sq, cq, dtau);
-        if (g >= 1) {
+        if (cq_col < N) {
 #pragma unroll
-            for (int r = 0; r < 7; r++) {
+            for (int r = 0; r < N; r++) {
                 float acc = 0.0f;
 #pragma unroll
-                for (int k = 0; k < 7; k++) acc = fmaf(mrow[r][k], dtau[k], acc);
-                gs->out[ks][7 * cq_col + r] = -acc;
+                for (int k = 0; k < N; k++) acc = fmaf(mrow[r][k], dtau[k], acc);
+                gs->out[ks][N * cq_col + r] = -acc;
             }
-        } else if constexpr (kDqColumn0Zero) {
+        } else if (kDqColumn0Zero && g == 0) {
 #pragma unroll
-            for (int r = 0; r < 7; r++) gs->out[ks][r] = 0.0f;  // dq column 0 is identically zero
+            for (int r = 0; r < N; r++) gs->out[ks][r] = 0.0f;  // dq column 0 is identically zero
         }
     }
     __syncwarp();
     // write the knot's outputs: group lanes stride over its floats
     if (kp.q) {
-        for (int e = g; e < 98; e += kGroupLanes) kp.dqdd[e] = gs->out[ks][e];
-        for (int e = g; e < 49; e += kGroupLanes) kp.minv[e] = gs->minv[ks][e];
-        if (g < 7) kp.qdd[g] = gs->qdd[ks][g];
+        for (int e = g; e < kDqddN; e += kGroupLanes) kp.dqdd[e] = gs->out[ks][e];
+        for (int e = g; e < NN; e += kGroupLanes) kp.minv[e] = gs->minv[ks][e];
+        if (g < N) kp.qdd[g] = gs->qdd[ks][g];
         if constexpr (MIRROR) {
             if (mr.dqdd) {
-                for (int e = g; e < 98; e += kGroupLanes) mr.dqdd[e] = gs->out[ks][e];
-                for (int e = g; e < 49; e += kGroupLanes) mr.minv[e] = gs->minv[ks][e];
-                if (g < 7) mr.qdd[g] = gs->qdd[ks][g];
+                for (int e = g; e < kDqddN; e += kGroupLanes) mr.dqdd[e] = gs->out[ks][e];
+                for (int e = g; e < NN; e += kGroupLanes) mr.minv[e] = gs->minv[ks][e];
+                if (g < N) mr.qdd[g] = gs->qdd[ks][g];
             }
         }
     }

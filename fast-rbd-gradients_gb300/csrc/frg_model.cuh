@@ -15,6 +15,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "frg_dims.h"
+
 // Scalar type of the device code: float for the engine; the FP64 verification
 // build (frg_f64_kernels.cu) compiles the same code with FRG_REAL=double into
 // namespace frg64.
@@ -33,7 +35,7 @@ __device__ __forceinline__ real fmaR(real a, real b, real c) {
     else return fma(a, b, c);
 }
 
-constexpr int kJoints = 7;
+constexpr int kJoints = FRG_MODEL_NUM_JOINTS;
 constexpr real kGravity = real(9.81);  // GRAVITY default, dynamicsGradient.h:7-9
 
 template <int N> struct IC { static constexpr int value = N; };

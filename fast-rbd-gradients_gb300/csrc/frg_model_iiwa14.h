@@ -7,6 +7,7 @@
  * vanish identically. */
 #pragma once
 #define FRG_MODEL_NAME "iiwa_14"
+#define FRG_MODEL_NUM_JOINTS 7
 #define FRG_MODEL_DQ_COLUMN0_ZERO 1
 #define FRG_MODEL_JOINT_F { \
     {1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0}, \

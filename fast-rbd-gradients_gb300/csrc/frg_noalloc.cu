@@ -115,7 +115,7 @@ extern "C" frg_status frg_gradient_ragged_noalloc(frg_ctx *ctx, int n_traj, cons
     // descriptors of the trajectories (same layout as the batched path)
     for (int t = 0; t < n_traj; t++) {
         const int64_t o = offsets[t];
-        h_segs[t] = frg::Segment{q + 7 * o, qd + 7 * o, u + 7 * o, dqdd + 98 * o, qdd + 7 * o, minv + 49 * o, o};
+        h_segs[t] = frg::Segment{q + frg::kN * o, qd + frg::kN * o, u + frg::kN * o, dqdd + frg::kDqddN * o, qdd + frg::kN * o, minv + frg::kMinvN * o, o};
     }
     h_segs[n_traj] = frg::Segment{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, total};
     const int ntiles = static_cast<int>((total + 31) / 32);

@@ -135,22 +135,24 @@ frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s)
     }
     DeviceGuard g(ctx->device);
     const size_t n = static_cast<size_t>(n_knots);
-    std::vector<float> h(21 * n);
+    using frg::kN;
+    std::vector<float> h(3 * kN * n);
     std::mt19937 rng(12345);
     std::uniform_real_distribution<float> uq(-2.0f, 2.0f), uu(-20.0f, 20.0f);
-    for (size_t i = 0; i < 14 * n; i++) h[i] = uq(rng);
-    for (size_t i = 14 * n; i < 21 * n; i++) h[i] = uu(rng);
+    for (size_t i = 0; i < 2 * kN * n; i++) h[i] = uq(rng);
+    for (size_t i = 2 * kN * n; i < 3 * kN * n; i++) h[i] = uu(rng);
     float *d = nullptr;
-    if (cudaMalloc(&d, sizeof(float) * 175 * n) != cudaSuccess) {
+    if (cudaMalloc(&d, sizeof(float) * frg::kSlotN * n) != cudaSuccess) {
         cudaGetLastError();
         frg_set_error(ctx, "frg_autotune: out of device memory");
         return FRG_ERR_OUT_OF_MEMORY;
     }
-    frg_traj tr{n_knots, d, d + 7 * n, d + 14 * n, d + 21 * n, d + 119 * n, d + 126 * n};
+    frg_traj tr{n_knots, d, d + frg::kSlotQd * n, d + frg::kSlotU * n, d + frg::kSlotDqdd * n,
+                d + frg::kSlotQdd * n, d + frg::kSlotMinv * n};
     std::string err;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaStream_t s = ctx->io_stream;
-    bool good = ok(ctx, cudaMemcpy(d, h.data(), sizeof(float) * 21 * n, cudaMemcpyHostToDevice), "autotune upload") &&
+    bool good = ok(ctx, cudaMemcpy(d, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice), "autotune upload") &&
                 ok(ctx, cudaEventCreate(&e0), "cudaEventCreate") && ok(ctx, cudaEventCreate(&e1), "cudaEventCreate");
     const frg::LaunchShape saved = ctx->shape, saved_r = ctx->ragged_shape;
     auto time_ms = [&](auto launch) {
@@ -187,8 +189,8 @@ frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s)
     std::vector<frg_traj> scattered;
     for (size_t k0 = 0; k0 < n; k0 += 128) {
         const size_t m = std::min<size_t>(128, n - k0);
-        scattered.push_back(frg_traj{static_cast<int64_t>(m), d + 7 * k0, d + 7 * n + 7 * k0, d + 14 * n + 7 * k0,
-                                     d + 21 * n + 98 * k0, d + 119 * n + 7 * k0, d + 126 * n + 49 * k0});
+        scattered.push_back(frg_traj{static_cast<int64_t>(m), tr.q + kN * k0, tr.qd + kN * k0, tr.u + kN * k0,
+                                     tr.dqdd + frg::kDqddN * k0, tr.qdd + kN * k0, tr.minv + frg::kMinvN * k0});
     }
     std::reverse(scattered.begin(), scattered.end());
     HostBatch hs;

@@ -10,14 +10,14 @@ namespace frg {
 // mirror into the device slot and the host-slot results (mr, null where not
 // wanted).
 __device__ __forceinline__ void serve_knot(const ServeSegment &sg, long long i, KnotPtrs &kp, KnotPtrs &mr) {
-    const long long h = sg.h;
+    const long long h = sg.h;  // each block of the slot is h knots long
     float *d = sg.dev, *hs = sg.host;
-    kp = KnotPtrs{sg.q + 7 * i, sg.qd + 7 * i, sg.u + 7 * i, d + 21 * h + 98 * i, d + 119 * h + 7 * i,
-                  d + 126 * h + 49 * i};
+    kp = KnotPtrs{sg.q + kN * i, sg.qd + kN * i, sg.u + kN * i, d + kSlotDqdd * h + kDqddN * i,
+                  d + kSlotQdd * h + kN * i, d + kSlotMinv * h + kMinvN * i};
     const bool mirror_in = sg.q != d;
-    mr = KnotPtrs{mirror_in ? d + 7 * i : nullptr, mirror_in ? d + 7 * h + 7 * i : nullptr,
-                  mirror_in ? d + 14 * h + 7 * i : nullptr, hs ? hs + 21 * h + 98 * i : nullptr,
-                  hs ? hs + 119 * h + 7 * i : nullptr, hs ? hs + 126 * h + 49 * i : nullptr};
+    mr = KnotPtrs{mirror_in ? d + kN * i : nullptr, mirror_in ? d + kSlotQd * h + kN * i : nullptr,
+                  mirror_in ? d + kSlotU * h + kN * i : nullptr, hs ? hs + kSlotDqdd * h + kDqddN * i : nullptr,
+                  hs ? hs + kSlotQdd * h + kN * i : nullptr, hs ? hs + kSlotMinv * h + kMinvN * i : nullptr};
 }
 
 }  // namespace frg

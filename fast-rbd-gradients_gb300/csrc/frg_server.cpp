@@ -2,8 +2,8 @@
 //
 // Requests are gradient calls of trajectories (MPC / iLQR style: one
 // trajectory makes many calls).  Each trajectory holds, from its first call to
-// frg_server_release, a slot of 175 floats per knot ([q | qd | u | dqdd | qdd
-// | minv]) in a capped device pool, mirrored at the same offset in a pinned
+// frg_server_release, a slot of 4N + 3N^2 floats per knot (175 for 7 joints:
+// [q | qd | u | dqdd | qdd | minv]) in a capped device pool, mirrored at the same offset in a pinned
 // host arena.  Admission is by free pool bytes: a trajectory whose slot does
 // not fit waits (an admission stall) until releases free enough of the pool.
 //
@@ -44,7 +44,7 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 constexpr size_t kGranule = 256;
-constexpr size_t kFloatsPerKnot = 175;
+constexpr size_t kFloatsPerKnot = frg::kSlotN;
 constexpr int kIdleSpinUs = 200;
 
 double us_between(Clock::time_point a, Clock::time_point b) {
@@ -197,16 +197,16 @@ void fill_info(const frg_server *s, const Request &r, frg_request_info *info) {
             const float *hs = s->host_slot(t), *ds = s->dev_slot(t);
             const int64_t h = t.h;
             if (r.host_results) {
-                info->dqdd = hs + 21 * h;
-                info->qdd = hs + 119 * h;
-                info->minv = hs + 126 * h;
+                info->dqdd = hs + frg::kSlotDqdd * h;
+                info->qdd = hs + frg::kSlotQdd * h;
+                info->minv = hs + frg::kSlotMinv * h;
             }
             info->dev_q = ds;
-            info->dev_qd = ds + 7 * h;
-            info->dev_u = ds + 14 * h;
-            info->dev_dqdd = ds + 21 * h;
-            info->dev_qdd = ds + 119 * h;
-            info->dev_minv = ds + 126 * h;
+            info->dev_qd = ds + frg::kSlotQd * h;
+            info->dev_u = ds + frg::kSlotU * h;
+            info->dev_dqdd = ds + frg::kSlotDqdd * h;
+            info->dev_qdd = ds + frg::kSlotQdd * h;
+            info->dev_minv = ds + frg::kSlotMinv * h;
         }
     }
 }
@@ -275,7 +275,7 @@ void frg_server::run() {
             Traj &t = trajs[r->traj];
             if (!admit(t, r->h)) break;
             if (r->src == Source::Host)
-                std::memcpy(host_slot(t), r->staged.data(), sizeof(float) * 21 * static_cast<size_t>(r->h));
+                std::memcpy(host_slot(t), r->staged.data(), sizeof(float) * 3 * frg::kN * static_cast<size_t>(r->h));
             r->staged.clear();
             r->staged.shrink_to_fit();
             r->state = ReqState::Ready;
@@ -334,12 +334,12 @@ void frg_server::launch_batch(Batch &b, std::unique_lock<std::mutex> &lk) {
         const float *q = r->dq, *qd = r->dqd, *u = r->du;  // Source::Device
         if (r->src == Source::Host) {
             q = hs;
-            qd = hs + 7 * h;
-            u = hs + 14 * h;
+            qd = hs + frg::kSlotQd * h;
+            u = hs + frg::kSlotU * h;
         } else if (r->src == Source::Resident) {
             q = ds;
-            qd = ds + 7 * h;
-            u = ds + 14 * h;
+            qd = ds + frg::kSlotQd * h;
+            u = ds + frg::kSlotU * h;
         }
         h_segs[i] = frg::ServeSegment{q, qd, u, ds, r->host_results ? hs : nullptr, h, begin};
         begin += r->h;
@@ -498,7 +498,7 @@ frg_status submit_call(frg_server *s, const char *who, uint64_t traj_id, int64_t
         horizon = it->second.h;
     }
     const size_t bytes = kFloatsPerKnot * sizeof(float) * static_cast<size_t>(horizon);
-    const size_t n7 = 7 * static_cast<size_t>(horizon);  // floats of one input array
+    const size_t n7 = frg::kN * static_cast<size_t>(horizon);  // floats of one input array
     if (bytes > s->arena.cap()) {
         s->st.rejected++;
         frg_set_error(s->ctx, std::string(who) + ": horizon " + std::to_string(horizon) +
@@ -601,11 +601,11 @@ frg_status frg_server_slot(frg_server *s, uint64_t traj_id, frg_slot_info *out) 
     const int64_t h = t.h;
     out->horizon = h;
     out->q = ds;
-    out->qd = ds + 7 * h;
-    out->u = ds + 14 * h;
-    out->dqdd = ds + 21 * h;
-    out->qdd = ds + 119 * h;
-    out->minv = ds + 126 * h;
+    out->qd = ds + frg::kSlotQd * h;
+    out->u = ds + frg::kSlotU * h;
+    out->dqdd = ds + frg::kSlotDqdd * h;
+    out->qdd = ds + frg::kSlotQdd * h;
+    out->minv = ds + frg::kSlotMinv * h;
     return FRG_OK;
 }
 

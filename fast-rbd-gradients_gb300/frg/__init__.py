@@ -15,6 +15,7 @@ from .native import (  # noqa: F401
     FrgError,
     Plan,
     Server,
+    dims,
     forward_dynamics_gradient,
     lib,
     model_name,

@@ -14,6 +14,7 @@ import os
 
 from .build import LIB_PATH
 
+# per-knot sizes of the default (iiwa_14) build; dims() gives the loaded library's
 NUM_JOINTS = 7
 DQDD_FLOATS = 98
 MINV_FLOATS = 49
@@ -37,6 +38,7 @@ EXPORTED = (
     "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64", "frg_get_tuning",
     "frg_set_tuning", "frg_knot_status", "frg_model_name", "frg_gradient_knots", "frg_server_cancel",
     "frg_single_knot_latency", "frg_server_submit_device", "frg_server_submit_resident", "frg_server_slot",
+    "frg_model_dofs",
 )
 SERVE_HOST_RESULTS = 1
 
@@ -151,6 +153,7 @@ def _declare(L):
                                           ctypes.POINTER(ctypes.c_uint64)]),
         "frg_server_submit_resident": (st, [vp, ctypes.c_uint64, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint64)]),
         "frg_server_slot": (st, [vp, ctypes.c_uint64, ctypes.POINTER(SlotInfo)]),
+        "frg_model_dofs": (i32, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -169,6 +172,13 @@ def lib():
         _declare(L)
         _lib = L
     return _lib
+
+
+def dims():
+    """(N, 2 N^2, N^2): joints, gradient floats and Minv floats per knot of the
+    loaded library (the robot it was built for)."""
+    n = lib().frg_model_dofs()
+    return n, 2 * n * n, n * n
 
 
 def model_name():
@@ -364,13 +374,14 @@ class Context:
                                             _ptr(qdd), _ptr(minv)), "frg_gradient_host")
 
     def gradient_host(self, q, qd, u):
-        """numpy float32 [n,7] x3 -> (dqdd [n,98], qdd [n,7], minv [n,49])."""
+        """numpy float32 [n,N] x3 -> (dqdd [n,2N^2], qdd [n,N], minv [n,N^2])."""
         import numpy as np
         q, qd, u = (np.ascontiguousarray(x, dtype=np.float32) for x in (q, qd, u))
         n = q.shape[0]
-        dqdd = np.empty((n, DQDD_FLOATS), np.float32)
-        qdd = np.empty((n, NUM_JOINTS), np.float32)
-        minv = np.empty((n, MINV_FLOATS), np.float32)
+        nj, nd, nm = dims()
+        dqdd = np.empty((n, nd), np.float32)
+        qdd = np.empty((n, nj), np.float32)
+        minv = np.empty((n, nm), np.float32)
         self.gradient_host_into(n, q, qd, u, dqdd, qdd, minv)
         return dqdd, qdd, minv
 
@@ -491,30 +502,32 @@ class Server:
 
     @staticmethod
     def results(info):
-        """Copies of (dqdd [h,98], qdd [h,7], minv [h,49]) from a completed call's info."""
+        """Copies of (dqdd [h,2N^2], qdd [h,N], minv [h,N^2]) from a completed call's info."""
         import numpy as np
         h = info.horizon
+        nj, nd, nm = dims()
         return tuple(np.ctypeslib.as_array(p, shape=(h, w)).copy()
-                     for p, w in ((info.dqdd, DQDD_FLOATS), (info.qdd, NUM_JOINTS), (info.minv, MINV_FLOATS)))
+                     for p, w in ((info.dqdd, nd), (info.qdd, nj), (info.minv, nm)))
 
 
 def forward_dynamics_gradient(q, qd, u, vel_damping=False, mpc_mode=False, ctx=None, stream=None):
-    """Batch gradient on torch CUDA tensors [n,7] (float32): returns
-    (dqdd [n,98], qdd [n,7], minv [n,49]) on the same device, asynchronously
-    on `stream` (default: torch's current stream)."""
+    """Batch gradient on torch CUDA tensors [n,N] (float32): returns
+    (dqdd [n,2N^2], qdd [n,N], minv [n,N^2]) on the same device,
+    asynchronously on `stream` (default: torch's current stream)."""
     import torch
+    nj, nd, nm = dims()
     for t in (q, qd, u):
-        if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and t.shape[-1] == NUM_JOINTS):
-            raise ValueError("q, qd, u must be contiguous float32 CUDA tensors of shape [n, 7]")
+        if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and t.shape[-1] == nj):
+            raise ValueError(f"q, qd, u must be contiguous float32 CUDA tensors of shape [n, {nj}]")
     n = q.shape[0]
     dev = q.device
     own = ctx is None
     if own:
         ctx = Context(device=dev.index or 0, vel_damping=vel_damping, mpc_mode=mpc_mode)
     try:
-        dqdd = torch.empty((n, DQDD_FLOATS), device=dev, dtype=torch.float32)
-        qdd = torch.empty((n, NUM_JOINTS), device=dev, dtype=torch.float32)
-        minv = torch.empty((n, MINV_FLOATS), device=dev, dtype=torch.float32)
+        dqdd = torch.empty((n, nd), device=dev, dtype=torch.float32)
+        qdd = torch.empty((n, nj), device=dev, dtype=torch.float32)
+        minv = torch.empty((n, nm), device=dev, dtype=torch.float32)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
         ctx.gradient(n, q, qd, u, dqdd, qdd, minv, stream=st)
         if own:

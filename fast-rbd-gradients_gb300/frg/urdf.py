@@ -8,9 +8,10 @@ cost nothing at run time.  This module writes that header from a URDF:
     python -m frg.urdf robot.urdf -o robot_tables.h [--name NAME]
     FRG_MODEL_TABLES=$PWD/robot_tables.h python -c "import __graft_entry__ as g; g.build()"
 
-Accepted robots: a fixed base followed by a serial chain of exactly 7
-revolute (or continuous) joints -- the per-knot sizes of the C ABI (7x14
-gradient, 7x7 Minv) are those of a 7-joint arm.  Fixed joints are merged:
+Accepted robots: a fixed base followed by a serial chain of 1 to 8 revolute
+(or continuous) joints; the header records the joint count N, and the
+library built from it has the per-knot sizes of an N-joint arm (N x 2N
+gradient, N x N Minv; frg_model_dofs() reports N).  Fixed joints are merged:
 links rigidly attached before the first joint are part of the fixed base,
 links rigidly attached to a moving link add their inertia to it.  Any joint
 axis is accepted: each moving frame is re-oriented so that its joint turns
@@ -31,7 +32,7 @@ import xml.etree.ElementTree as ET
 
 import numpy as np
 
-NUM_JOINTS = 7
+MAX_JOINTS = 8  # the latency mapping gives each joint a lane of its 8
 _SNAP = 1e-12
 
 
@@ -177,8 +178,8 @@ def parse(text):
         inertials.append(Inertial())
         moving = len(out_joints) - 1
         link = j.find("child").get("link")
-    if len(out_joints) != NUM_JOINTS:
-        raise ValueError(f"the kernels take {NUM_JOINTS} moving joints; this chain has {len(out_joints)}")
+    if not 1 <= len(out_joints) <= MAX_JOINTS:
+        raise ValueError(f"the kernels take 1 to {MAX_JOINTS} moving joints; this chain has {len(out_joints)}")
     return {"name": root.get("name", "robot"), "joints": out_joints, "inertials": inertials}
 
 
@@ -220,6 +221,7 @@ def emit_header(t, source="a URDF"):
  * vanish identically. */
 #pragma once
 #define FRG_MODEL_NAME "{t['name']}"
+#define FRG_MODEL_NUM_JOINTS {len(t['F'])}
 #define FRG_MODEL_DQ_COLUMN0_ZERO {1 if t['dq_column0_zero'] else 0}
 #define FRG_MODEL_JOINT_F {{ \\
 {rows(t['F'])} }}

@@ -93,6 +93,7 @@ double pct(std::vector<double> &v, double p) {
 
 extern "C" int frg_loadgen_run(frg_server *srv, const frg_loadgen_cfg *cfg, frg_loadgen_result *res) {
     if (!srv || !cfg || !res || cfg->calls < 1 || cfg->threads < 1) return 1;
+    if (frg_model_dofs() != 7) return 1;  // the sessions sample the iiwa_14's joint limits
     std::memset(res, 0, sizeof(*res));
     const float lim[7] = {2.96705972839f, 2.09439510239f, 2.96705972839f, 2.09439510239f,
                           2.96705972839f, 2.09439510239f, 3.05432619099f};

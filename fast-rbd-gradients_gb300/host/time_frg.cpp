@@ -144,6 +144,11 @@ void print_mat(const float *A, int rows, int cols, int lda) {
 }  // namespace
 
 int main(int argc, char **argv) {
+    if (frg_model_dofs() != 7) {  // this driver mirrors time_GPU.cu, whose model is the 7-joint iiwa_14
+        std::fprintf(stderr, "time_frg drives the iiwa_14 build; this library is %s with %d joints\n",
+                     frg_model_name(), frg_model_dofs());
+        return 2;
+    }
     int iters = 1000;
     bool equivalence = false, autotune = false;
     int ragged = 0;

@@ -15,14 +15,17 @@
  * forwardDynamics (helpers_CPU/dynamicsGradient.h:686-706, :936-939).
  *
  * Layouts (all float32, knot-major, every matrix column-major as in the
- * reference, helpers_CPU/dynamicsGradient.h:34-41):
- *   q, qd, u  [n][7]
- *   dqdd      [n][98]  = 7x14, column c < 7: dq̈/dq_c, column 7 + c: dq̈/dq̇_c
+ * reference, helpers_CPU/dynamicsGradient.h:34-41), for a robot of N joints
+ * (N = 7 for the iiwa_14; frg_model_dofs() reports the build's N, as the
+ * reference's NUM_POS macro fixes it, dynamicsGradient.h:7-12):
+ *   q, qd, u  [n][N]
+ *   dqdd      [n][2N^2] = N x 2N, column c < N: dq̈/dq_c, column N + c: dq̈/dq̇_c
  *                        (the reference's 2*NUM_POS*NUM_POS block per knot,
- *                        time_CPU.cpp:34, dynamicsGradient.h:921)
- *   qdd       [n][7]
- *   minv      [n][49]  dense symmetric (the reference's DENSE_MINV form,
- *                        time_GPU.cu:134)
+ *                        time_CPU.cpp:34, dynamicsGradient.h:921; 98 floats)
+ *   qdd       [n][N]
+ *   minv      [n][N^2]  dense symmetric (the reference's DENSE_MINV form,
+ *                        time_GPU.cu:134; 49 floats)
+ * Sizes below quoted as numbers are the iiwa's (N = 7).
  *
  * Conventions: every call returns an frg_status (nothing aborts or exits;
  * the reference's gpuErrchk aborted the process, dynamicsGradient.cuh:28-35);
@@ -39,6 +42,9 @@
 extern "C" {
 #endif
 
+/* Per-knot sizes of the default build (the 7-joint iiwa_14).  A library built
+ * for another robot reports its joint count N through frg_model_dofs(); its
+ * sizes are those of the layouts above with that N. */
 #define FRG_NUM_JOINTS 7
 #define FRG_DQDD_FLOATS 98
 #define FRG_MINV_FLOATS 49
@@ -83,8 +89,11 @@ const char *frg_status_string(frg_status s);
 /* The robot this library was built for: "iiwa_14" (the default, the
  * reference's model, code-generated there at helpers_CPU/dynamicsGradient.h:
  * 124-229) or the name in the tables header frg/urdf.py wrote from another
- * URDF of a 7-joint serial arm. */
+ * URDF of a serial arm of 1 to 8 revolute joints. */
 const char *frg_model_name(void);
+/* Its joint count N (7 for the iiwa_14): the reference's NUM_POS
+ * (helpers_CPU/dynamicsGradient.h:7-12), which sizes every per-knot array. */
+int frg_model_dofs(void);
 
 /* Creates a context on opt->device (NULL opt = defaults). */
 frg_status frg_create(frg_ctx **out, const frg_options *opt);
@@ -140,8 +149,8 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
 
 /*
  * The reference's own per-knot layout, for callers that already pack it: the
- * knot<T> record of helpers_CPU/dynamicsGradient.h:19-25, [q 7 | qd 7 | u 7 |
- * qdd 7 | Minv 49] = FRG_KNOT_RECORD_FLOATS floats per knot, as time_GPU.cu:
+ * knot<T> record of helpers_CPU/dynamicsGradient.h:19-25, [q N | qd N | u N |
+ * qdd N | Minv N^2] = FRG_KNOT_RECORD_FLOATS (4N + N^2) floats per knot, as time_GPU.cu:
  * 137-158 packs it for dynamicsGradientKernel.  knots [n] (DEVICE) supply q,
  * qd, u; q̈ and dense Minv are written into each record's qdd and Minv fields
  * (the reference fills them on the host first, forwardDynamics at

@@ -35,9 +35,16 @@ static const double kGravity = 9.81;
 #else
 #include "../fast-rbd-gradients_gb300/csrc/frg_model_iiwa14.h"
 #endif
-static const double kLinkInertial[7][10] = FRG_MODEL_LINK_INERTIAL;
-static const double kJointFT[7][9] = FRG_MODEL_JOINT_F;
-static const double kJointOrigin[7][3] = FRG_MODEL_JOINT_ORIGIN;
+#ifndef FRG_MODEL_NUM_JOINTS
+#define FRG_MODEL_NUM_JOINTS 7
+#endif
+/* per-knot sizes for N joints: q, qd, u, qdd N; dqdd 2N^2; Minv N^2; fext 6N */
+#define KN FRG_MODEL_NUM_JOINTS
+#define KD (2 * KN * KN)
+#define KM (KN * KN)
+static const double kLinkInertial[KN][10] = FRG_MODEL_LINK_INERTIAL;
+static const double kJointFT[KN][9] = FRG_MODEL_JOINT_F;
+static const double kJointOrigin[KN][3] = FRG_MODEL_JOINT_ORIGIN;
 
 #define REAL double
 #define FN(name) name##_f64
@@ -54,12 +61,15 @@ static const double kJointOrigin[7][3] = FRG_MODEL_JOINT_ORIGIN;
 
 /* -------------------------------------------------------------- exports ---- */
 
+/* Joint count N of the model compiled in (the per-knot sizes follow it). */
+int frg_oracle_dofs(void) { return KN; }
+
 int frg_oracle_gradient_f64(int n, const double *q, const double *qd, const double *u, const double *fext,
                             int damping, int mpc, double *dqdd, double *qdd, double *minv) {
     if (n < 0) return 1;
     for (int k = 0; k < n; k++)
-        knot_gradient_f64(&q[7 * k], &qd[7 * k], &u[7 * k], fext ? &fext[42 * k] : NULL, damping, mpc,
-                          &dqdd[98 * k], &qdd[7 * k], &minv[49 * k]);
+        knot_gradient_f64(&q[KN * k], &qd[KN * k], &u[KN * k], fext ? &fext[6 * KN * k] : NULL, damping, mpc,
+                          &dqdd[KD * k], &qdd[KN * k], &minv[KM * k]);
     return 0;
 }
 
@@ -67,15 +77,15 @@ int frg_oracle_gradient_f32(int n, const float *q, const float *qd, const float 
                             int damping, int mpc, float *dqdd, float *qdd, float *minv) {
     if (n < 0) return 1;
     for (int k = 0; k < n; k++)
-        knot_gradient_f32(&q[7 * k], &qd[7 * k], &u[7 * k], fext ? &fext[42 * k] : NULL, damping, mpc,
-                          &dqdd[98 * k], &qdd[7 * k], &minv[49 * k]);
+        knot_gradient_f32(&q[KN * k], &qd[KN * k], &u[KN * k], fext ? &fext[6 * KN * k] : NULL, damping, mpc,
+                          &dqdd[KD * k], &qdd[KN * k], &minv[KM * k]);
     return 0;
 }
 
 /* Transforms and inertias alone, for the model-constant checks. */
 void frg_oracle_model_f64(const double *q, double *X, double *I) {
-    double s[7], c[7];
-    for (int k = 0; k < 7; k++) { s[k] = sin(q[k]); c[k] = cos(q[k]); }
+    double s[KN], c[KN];
+    for (int k = 0; k < KN; k++) { s[k] = sin(q[k]); c[k] = cos(q[k]); }
     model_transforms_f64(X, s, c);
     model_inertias_f64(I);
 }
@@ -113,11 +123,11 @@ static void *worker_main(void *arg) {
         const int per = n / T, k0 = per * w->tid, k1 = (w->tid == T - 1) ? n : per * (w->tid + 1);
         if (k1 > k0 && given) {
             for (int k = k0; k < k1; k++)
-                knot_gradient_given_f32(g_pool.q + 7 * k, g_pool.qd + 7 * k, g_pool.qdd + 7 * k,
-                                        g_pool.minv + 49 * k, 0, 0, g_pool.dqdd + 98 * k);
+                knot_gradient_given_f32(g_pool.q + KN * k, g_pool.qd + KN * k, g_pool.qdd + KN * k,
+                                        g_pool.minv + KM * k, 0, 0, g_pool.dqdd + KD * k);
         } else if (k1 > k0) {
-            frg_oracle_gradient_f32(k1 - k0, g_pool.q + 7 * k0, g_pool.qd + 7 * k0, g_pool.u + 7 * k0, NULL, 0, 0,
-                                    g_pool.dqdd + 98 * k0, g_pool.qdd + 7 * k0, g_pool.minv + 49 * k0);
+            frg_oracle_gradient_f32(k1 - k0, g_pool.q + KN * k0, g_pool.qd + KN * k0, g_pool.u + KN * k0, NULL, 0, 0,
+                                    g_pool.dqdd + KD * k0, g_pool.qdd + KN * k0, g_pool.minv + KM * k0);
         }
         pthread_mutex_lock(&g_pool.mu);
         if (--g_pool.pending == 0) pthread_cond_signal(&g_pool.done);
@@ -190,7 +200,7 @@ int frg_oracle_gradient_given_f32(int n, const float *q, const float *qd, const 
                                   float *dqdd) {
     if (n < 0) return 1;
     for (int k = 0; k < n; k++)
-        knot_gradient_given_f32(&q[7 * k], &qd[7 * k], &qdd[7 * k], &minv[49 * k], 0, 0, &dqdd[98 * k]);
+        knot_gradient_given_f32(&q[KN * k], &qd[KN * k], &qdd[KN * k], &minv[KM * k], 0, 0, &dqdd[KD * k]);
     return 0;
 }
 

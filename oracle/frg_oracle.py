@@ -45,6 +45,8 @@ def _load():
         L.frg_oracle_gradient_given_f32.restype = i
         L.frg_oracle_model_f64.argtypes = [vp, vp, vp]
         L.frg_oracle_pool_shutdown.argtypes = []
+        L.frg_oracle_dofs.argtypes = []
+        L.frg_oracle_dofs.restype = i
         _oracle = L
     return _oracle
 
@@ -67,10 +69,10 @@ def _load_ref():
 
 def _run(fn, dtype, q, qd, u, damping, mpc, fext=None, with_fext=True):
     q, qd, u = (np.ascontiguousarray(x, dtype=dtype) for x in (q, qd, u))
-    n = q.shape[0]
-    dqdd = np.zeros((n, 98), dtype)
-    qdd = np.zeros((n, 7), dtype)
-    minv = np.zeros((n, 49), dtype)
+    n, nj = q.shape[0], q.shape[1]
+    dqdd = np.zeros((n, 2 * nj * nj), dtype)
+    qdd = np.zeros((n, nj), dtype)
+    minv = np.zeros((n, nj * nj), dtype)
     args = [n, q.ctypes.data, qd.ctypes.data, u.ctypes.data]
     if with_fext:
         fx = None if fext is None else np.ascontiguousarray(fext, dtype=dtype)

@@ -12,7 +12,7 @@
  */
 
 #define SZ6 6
-#define NJ 7
+#define NJ FRG_MODEL_NUM_JOINTS
 
 /* ---------------------------------------------------------------- model ---- */
 
@@ -41,7 +41,7 @@ static void FN(spatial_inertia)(REAL *I, const double p[10]) {
     I[3 + 6 * 3] = I[4 + 6 * 4] = I[5 + 6 * 5] = m;
 }
 
-/* All 7 link inertias (initInertiaTensors, dynamicsGradient.h:124-212). */
+/* All NJ link inertias (initInertiaTensors, dynamicsGradient.h:124-212). */
 static void FN(model_inertias)(REAL *I) {
     for (int k = 0; k < NJ; k++) FN(spatial_inertia)(&I[36 * k], kLinkInertial[k]);
 }
@@ -331,7 +331,8 @@ static void FN(dtau_columns)(REAL *cdq, REAL *cdqd, const REAL *v, const REAL *a
  * QDD_MINV_PASSED_IN=false (dynamicsGradient.h:925-934 via :869-897):
  *   RNEA(q, qd, 0) -> bias = u - c (- 0.5 qd) -> Minv -> qdd = Minv bias
  *   -> RNEA(q, qd, qdd) -> d tau -> dqdd = -Minv [d tau/dq | d tau/dqd].
- * Outputs: dqdd[98] (7x14 column-major), qdd[7], Minv[49] dense. */
+ * Outputs: dqdd[2 NJ^2] (NJ x 2NJ column-major), qdd[NJ], Minv[NJ^2] dense
+ * (98, 7 and 49 floats for the 7-joint iiwa). */
 static void FN(knot_gradient)(const REAL *q, const REAL *qd, const REAL *u, const REAL *fext, int damping,
                               int mpc, REAL *dqdd, REAL *qdd, REAL *minv_dense) {
     REAL sq[NJ], cq[NJ], X[NJ * 36], I[NJ * 36];

@@ -1,6 +1,7 @@
 """Test helpers for URDF-generated models.
 
-synthetic_urdf(): a seeded 7-joint serial arm that exercises every general
+synthetic_urdf(): a seeded serial arm (7 joints by default, any count from 1
+to 8) that exercises every general
 form the kernels and the oracle take: frames at arbitrary roll/pitch/yaw,
 joint origins off the axes, joint axes other than z (one reversed), inertial
 frames with their own rotation, fixed links before the first joint and after
@@ -30,7 +31,7 @@ def _fmt(v):
     return " ".join(f"{x:.17g}" for x in v)
 
 
-def synthetic_urdf(seed=11, name="synthetic_arm"):
+def synthetic_urdf(seed=11, name="synthetic_arm", joints=7):
     rng = np.random.default_rng(seed)
     parts = [f'<robot name="{name}">', '<link name="world"/>',
              # a mount rigidly attached to the world: part of the fixed base
@@ -39,7 +40,7 @@ def synthetic_urdf(seed=11, name="synthetic_arm"):
              '<link name="pedestal"><inertial><origin xyz="0 0 0.1"/><mass value="9"/>'
              '<inertia ixx="1" ixy="0" ixz="0" iyy="1" iyz="0" izz="1"/></inertial></link>']
     parent = "pedestal"
-    for k in range(7):
+    for k in range(joints):
         axis = rng.normal(size=3)
         if k == 3:
             axis = np.array([0.0, 0.0, -1.0])  # reversed z
@@ -56,15 +57,15 @@ def synthetic_urdf(seed=11, name="synthetic_arm"):
                      f'rpy="{_fmt(_rpy(rng))}"/><mass value="{rng.uniform(0.8, 5.0):.17g}"/>'
                      f'<inertia ixx="{I[0, 0]:.17g}" ixy="{I[0, 1]:.17g}" ixz="{I[0, 2]:.17g}" '
                      f'iyy="{I[1, 1]:.17g}" iyz="{I[1, 2]:.17g}" izz="{I[2, 2]:.17g}"/></inertial></link>')
-        if k == 3:  # a welded sensor on link 4
-            parts.append(f'<joint name="sensor_mount" type="fixed"><parent link="l4"/><child link="sensor"/>'
+        if k == min(3, joints - 1):  # a welded sensor on link 4 (or the last)
+            parts.append(f'<joint name="sensor_mount" type="fixed"><parent link="l{k + 1}"/><child link="sensor"/>'
                          f'<origin xyz="{_fmt(rng.uniform(-0.1, 0.1, 3))}" rpy="{_fmt(_rpy(rng))}"/></joint>'
                          '<link name="sensor"><inertial><origin xyz="0.01 0.02 0.03" rpy="0.1 0.2 0.3"/>'
                          '<mass value="0.4"/><inertia ixx="0.001" ixy="0.0001" ixz="0" iyy="0.002" iyz="0" '
                          'izz="0.0015"/></inertial></link>')
         parent = f"l{k + 1}"
     # a tool rigidly attached to the last link, with a frame of its own
-    parts.append('<joint name="tool_mount" type="fixed"><parent link="l7"/><child link="tool"/>'
+    parts.append(f'<joint name="tool_mount" type="fixed"><parent link="l{joints}"/><child link="tool"/>'
                  f'<origin xyz="{_fmt(rng.uniform(-0.1, 0.1, 3))}" rpy="{_fmt(_rpy(rng))}"/></joint>'
                  '<link name="tool"><inertial><origin xyz="0 0 0.05" rpy="0 0.5 0"/><mass value="0.7"/>'
                  '<inertia ixx="0.003" ixy="0" ixz="0" iyy="0.004" iyz="0" izz="0.002"/></inertial></link>')
@@ -106,33 +107,40 @@ class NewtonEuler:
             F.append(ine.m * a_c)
             N.append(Iw @ dw + np.cross(w, Iw @ w))
             p = pj
-        tau = np.zeros(7)
+        nj = len(z)
+        tau = np.zeros(nj)
         f, n = np.zeros(3), np.zeros(3)
-        for k in range(6, -1, -1):
-            if k < 6:
+        for k in range(nj - 1, -1, -1):
+            if k < nj - 1:
                 n = n + np.cross(P[k + 1] - P[k], f)
             n = N[k] + n + np.cross(C[k] - P[k], F[k])
             f = F[k] + f
             tau[k] = z[k] @ n
         return tau
 
+    @property
+    def dofs(self):
+        return len(self.m["joints"])
+
     def mass_matrix(self, q):
-        Z = np.zeros(7)
-        return np.stack([self.tau(q, Z, np.eye(7)[j], gravity=False) for j in range(7)], axis=1)
+        nj = self.dofs
+        Z = np.zeros(nj)
+        return np.stack([self.tau(q, Z, np.eye(nj)[j], gravity=False) for j in range(nj)], axis=1)
 
     def forward(self, q, qd, u, gravity=True):
         M = self.mass_matrix(q)
-        qdd = np.linalg.solve(M, u - self.tau(q, qd, np.zeros(7), gravity))
+        qdd = np.linalg.solve(M, u - self.tau(q, qd, np.zeros(self.dofs), gravity))
         return qdd, np.linalg.inv(M)
 
     def gradient(self, q, qd, u, gravity=True, h=1e-6):
-        """[dqdd/dq | dqdd/dqd] (7x14) by central differences."""
-        G = np.zeros((7, 14))
-        for j in range(7):
-            e = np.zeros(7)
+        """[dqdd/dq | dqdd/dqd] (N x 2N) by central differences."""
+        nj = self.dofs
+        G = np.zeros((nj, 2 * nj))
+        for j in range(nj):
+            e = np.zeros(nj)
             e[j] = h
             G[:, j] = (self.forward(q + e, qd, u, gravity)[0] - self.forward(q - e, qd, u, gravity)[0]) / (2 * h)
-            G[:, 7 + j] = (self.forward(q, qd + e, u, gravity)[0] - self.forward(q, qd - e, u, gravity)[0]) / (2 * h)
+            G[:, nj + j] = (self.forward(q, qd + e, u, gravity)[0] - self.forward(q, qd - e, u, gravity)[0]) / (2 * h)
         return G
 
 
@@ -150,13 +158,15 @@ def build_oracle(header, out_so, root):
 
 
 def oracle_gradient_f64(so, q, qd, u, damping=0, mpc=0):
-    """dqdd [n,98], qdd [n,7], minv [n,49] from a model's oracle library."""
+    """dqdd [n,2N^2], qdd [n,N], minv [n,N^2] from a model's oracle library."""
     L = ctypes.CDLL(so)
     vp, i = ctypes.c_void_p, ctypes.c_int
     L.frg_oracle_gradient_f64.argtypes = [i, vp, vp, vp, vp, i, i, vp, vp, vp]
+    L.frg_oracle_dofs.restype = i
     q, qd, u = (np.ascontiguousarray(x, np.float64) for x in (q, qd, u))
-    n = q.shape[0]
-    out = [np.zeros((n, w)) for w in (98, 7, 49)]
+    n, nj = q.shape
+    assert nj == L.frg_oracle_dofs(), "inputs do not match the oracle's joint count"
+    out = [np.zeros((n, w)) for w in (2 * nj * nj, nj, nj * nj)]
     L.frg_oracle_gradient_f64(n, q.ctypes.data, qd.ctypes.data, u.ctypes.data, None, damping, mpc,
                               *(o.ctypes.data for o in out))
     return out

@@ -39,8 +39,10 @@ def _chain(joints, extra=""):
 
 
 def test_generator_rejects_what_the_kernels_cannot_take():
-    with pytest.raises(ValueError, match="7 moving joints"):
-        urdf.parse(_chain(["revolute"] * 6))
+    with pytest.raises(ValueError, match="1 to 8 moving joints"):
+        urdf.parse(_chain(["revolute"] * 9))
+    with pytest.raises(ValueError, match="1 to 8 moving joints"):
+        urdf.parse(_chain(["fixed"] * 2))
     with pytest.raises(ValueError, match="not supported"):
         urdf.parse(_chain(["revolute"] * 3 + ["prismatic"] + ["revolute"] * 3))
     branch = ('<joint name="extra" type="revolute"><parent link="l2"/><child link="x"/><axis xyz="0 0 1"/></joint>'
@@ -58,33 +60,44 @@ def test_generator_reorients_axes_and_merges_fixed_links():
     m = urdf.parse(synthetic_urdf())
     # link 4 carries the welded sensor, link 7 the tool
     assert m["inertials"][3].m > 0.4 and m["inertials"][6].m > 0.7
+    m6 = urdf.parse(synthetic_urdf(joints=6))
+    assert len(m6["joints"]) == 6 and m6["inertials"][5].m > 0.7
 
 
-@pytest.fixture(scope="module")
-def synthetic_oracle(tmp_path_factory):
-    d = tmp_path_factory.mktemp("model")
-    text = synthetic_urdf()
+@pytest.fixture(scope="module", params=[7, 6, 3, 8])
+def synthetic_oracle(tmp_path_factory, request):
+    joints = request.param
+    d = tmp_path_factory.mktemp(f"model{joints}")
+    text = synthetic_urdf(joints=joints)
     header = write_tables(text, str(d / "synthetic_tables.h"))
     return text, header, build_oracle(header, str(d / "liboracle_synthetic.so"), ROOT)
+
+
+def test_tables_carry_the_joint_count(synthetic_oracle):
+    text, header, _ = synthetic_oracle
+    nj = len(urdf.parse(text)["joints"])
+    assert f"#define FRG_MODEL_NUM_JOINTS {nj}" in open(header).read()
 
 
 @pytest.mark.parametrize("mpc", [0, 1])
 def test_oracle_for_generated_model_matches_newton_euler(synthetic_oracle, mpc):
     """q̈ and Minv of the oracle built for the generated tables equal those of
     the world-frame Newton-Euler model of the URDF (FP64, <= 1e-10), and its
-    gradient equals central differences of that model (<= 1e-6)."""
+    gradient equals central differences of that model (<= 1e-6), for arms of
+    7, 6, 3 and 8 joints."""
     text, _, so = synthetic_oracle
     ne = NewtonEuler(text)
+    nj = ne.dofs
     rng = np.random.default_rng(5 + mpc)
     n = 6
-    q, qd, u = rng.uniform(-2.5, 2.5, (n, 7)), rng.uniform(-2, 2, (n, 7)), rng.uniform(-20, 20, (n, 7))
+    q, qd, u = rng.uniform(-2.5, 2.5, (n, nj)), rng.uniform(-2, 2, (n, nj)), rng.uniform(-20, 20, (n, nj))
     dqdd, qdd, minv = oracle_gradient_f64(so, q, qd, u, mpc=mpc)
     for k in range(n):
         r_qdd, r_minv = ne.forward(q[k], qd[k], u[k], gravity=not mpc)
         assert np.linalg.norm(qdd[k] - r_qdd) <= 1e-10 * np.linalg.norm(r_qdd)
         assert np.linalg.norm(minv[k] - r_minv.T.reshape(-1)) <= 1e-10 * np.linalg.norm(r_minv)
         G = ne.gradient(q[k], qd[k], u[k], gravity=not mpc)
-        got = dqdd[k].reshape(14, 7).T  # column-major 7x14
+        got = dqdd[k].reshape(2 * nj, nj).T  # column-major N x 2N
         assert np.linalg.norm(got - G) <= 1e-6 * np.linalg.norm(G)
         if not mpc:  # the tilted base joint: column 0 of d qdd / dq lives
             assert np.linalg.norm(got[:, 0]) > 1e-3 * np.linalg.norm(G)
