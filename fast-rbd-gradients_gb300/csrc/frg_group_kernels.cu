@@ -50,31 +50,20 @@ __global__ void __launch_bounds__(32)
     }
 }
 
-// persistent: ticket -> (32-knot tile t, 4-knot slice s); the last ticket
-// (items + total_warps - 1) resets the counter, as in grad_ragged_kernel
+// persistent (next_ticket): ticket -> (32-knot tile t, 4-knot slice s)
 template <bool DAMP, bool MPC, bool SERVE, typename Seg>
 __device__ __forceinline__ void group_persistent(const Seg *segs, int nseg, const int *tile_seg, int ntiles,
                                                  unsigned int *counter) {
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     GroupSmem *gs = reinterpret_cast<GroupSmem *>(smem_raw) + warp;
-    const unsigned int total_warps = gridDim.x * (blockDim.x >> 5);
     const unsigned int items = static_cast<unsigned int>(ntiles) * 8u;
-    for (;;) {
-        unsigned int ticket = 0;
-        if (lane == 0) ticket = atomicAdd(counter, 1u);
-        ticket = __shfl_sync(0xffffffffu, ticket, 0);
-        if (ticket >= items) {
-            if (lane == 0 && ticket == items + total_warps - 1u) atomicExch(counter, 0u);
-            return;
-        }
+    for (unsigned int ticket; next_ticket(items, counter, lane, ticket);) {
         const int tile = static_cast<int>(ticket >> 3), slice = static_cast<int>(ticket & 7u);
         const long long g = static_cast<long long>(tile) * 32 + slice * kGroupKnots + (lane >> 3);
         KnotPtrs kp{}, mr{};
         if (g < segs[nseg].knot_begin) {
-            int s = tile_seg[tile];
-            while (s + 1 < nseg && segs[s + 1].knot_begin <= g) s++;
-            const Seg &sg = segs[s];
+            const Seg &sg = segs[segment_of(segs, nseg, tile_seg[tile], g)];
             const long long i = g - sg.knot_begin;
             if constexpr (SERVE) {
                 serve_knot(sg, i, kp, mr);

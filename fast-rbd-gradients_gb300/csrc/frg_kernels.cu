@@ -79,35 +79,21 @@ __device__ __forceinline__ KnotPtrs ragged_knot(const Segment *segs, int nseg, c
                                                 int lane) {
     const long long g = static_cast<long long>(tile) * 32 + lane;
     if (g >= segs[nseg].knot_begin) return KnotPtrs{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    int s = tile_seg[tile];
-    while (s + 1 < nseg && segs[s + 1].knot_begin <= g) s++;
-    const Segment &sg = segs[s];
+    const Segment &sg = segs[segment_of(segs, nseg, tile_seg[tile], g)];
     const long long i = g - sg.knot_begin;
     return KnotPtrs{sg.q + kN * i, sg.qd + kN * i, sg.u + kN * i, sg.dqdd + kDqddN * i, sg.qdd + kN * i, sg.minv + kMinvN * i};
 }
 
 // Persistent: each warp takes 32-knot tiles from a device work counter until
-// the list is exhausted.  The warp that draws the very last ticket
-// (ntiles + total_warps - 1: every warp fails exactly once) resets the counter,
-// so back-to-back and graph-replayed launches need no memset.
+// the list is exhausted (next_ticket).
 template <bool DAMP, bool MPC>
 __global__ void __launch_bounds__(kMaxWarpsPerCta * 32)
     grad_ragged_kernel(const Segment *segs, int nseg, const int *tile_seg, int ntiles, unsigned int *counter) {
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
-    const unsigned int total_warps = gridDim.x * (blockDim.x >> 5);
-    for (;;) {
-        unsigned int ticket = 0;
-        if (lane == 0) ticket = atomicAdd(counter, 1u);
-        ticket = __shfl_sync(0xffffffffu, ticket, 0);
-        if (ticket >= static_cast<unsigned int>(ntiles)) {
-            if (lane == 0 && ticket == static_cast<unsigned int>(ntiles) + total_warps - 1u) atomicExch(counter, 0u);
-            return;
-        }
-        const KnotPtrs kp = ragged_knot(segs, nseg, tile_seg, static_cast<int>(ticket), lane);
-        process_tile<DAMP, MPC>(ws, lane, kp);
-    }
+    for (unsigned int tile; next_ticket(static_cast<unsigned int>(ntiles), counter, lane, tile);)
+        process_tile<DAMP, MPC>(ws, lane, ragged_knot(segs, nseg, tile_seg, static_cast<int>(tile), lane));
 }
 
 // Single-knot latency (the reference's kern_single_full, time_GPU.cu:23-51,

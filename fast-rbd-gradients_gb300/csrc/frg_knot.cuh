@@ -63,6 +63,31 @@ struct KnotPtrs {
     const real *fext = nullptr;  // [kJoints][6] external spatial force per link (link frame), optional
 };
 
+// Persistent work loop: a warp draws tickets from a device counter,
+//     for (unsigned int t; next_ticket(items, counter, lane, t);) work(t);
+// until the `items` work items are exhausted.  The warp that draws the very
+// last ticket (items + total warps - 1: every warp draws one failing ticket)
+// resets the counter, so back-to-back and graph-replayed launches need no
+// memset.
+__device__ __forceinline__ bool next_ticket(unsigned int items, unsigned int *counter, int lane,
+                                            unsigned int &ticket) {
+    unsigned int t = 0;
+    if (lane == 0) t = atomicAdd(counter, 1u);
+    ticket = __shfl_sync(0xffffffffu, t, 0);
+    if (ticket < items) return true;
+    if (lane == 0 && ticket == items + gridDim.x * (blockDim.x >> 5) - 1u) atomicExch(counter, 0u);
+    return false;
+}
+
+// The segment of a ragged knot list that holds knot g (segs[nseg].knot_begin
+// is the total knot count, g below it): the last one starting at or before g,
+// searched upward from s, the segment of g's tile's first knot.
+template <typename Seg>
+__device__ __forceinline__ int segment_of(const Seg *segs, int nseg, int s, long long g) {
+    while (s + 1 < nseg && segs[s + 1].knot_begin <= g) s++;
+    return s;
+}
+
 __device__ __forceinline__ const real *shfl_ptr(const real *p, int src) {
     return reinterpret_cast<const real *>(
         __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), src));

@@ -17,20 +17,11 @@ __global__ void __launch_bounds__(8 * 32)
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
-    const unsigned int total_warps = gridDim.x * (blockDim.x >> 5);
-    for (;;) {
-        unsigned int ticket = 0;
-        if (lane == 0) ticket = atomicAdd(counter, 1u);
-        ticket = __shfl_sync(0xffffffffu, ticket, 0);
-        if (ticket >= static_cast<unsigned int>(ntiles)) {
-            if (lane == 0 && ticket == static_cast<unsigned int>(ntiles) + total_warps - 1u) atomicExch(counter, 0u);
-            return;
-        }
-        const long long g = static_cast<long long>(ticket) * 32 + lane;
+    for (unsigned int tile; next_ticket(static_cast<unsigned int>(ntiles), counter, lane, tile);) {
+        const long long g = static_cast<long long>(tile) * 32 + lane;
         KnotPtrs kp{}, mr{};
         if (g < segs[nseg].knot_begin) {
-            int s = tile_seg[ticket];
-            while (s + 1 < nseg && segs[s + 1].knot_begin <= g) s++;
+            const int s = segment_of(segs, nseg, tile_seg[tile], g);
             serve_knot(segs[s], g - segs[s].knot_begin, kp, mr);
         }
         process_tile<DAMP, MPC, true>(ws, lane, kp, mr);
