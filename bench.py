@@ -471,14 +471,17 @@ def run_frg(args):
         torch.cuda.synchronize(dev)
 
     def timed(fn, steps):
-        """Per-step CUDA-event times (ms) on `stream` for `steps` calls."""
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        """CUDA-event time (ms) on `stream` of `steps` calls issued back to
+        back between one pair of events, as a list of `steps` equal per-step
+        shares.  (Bracketing every step with its own events instead adds the
+        stream's event processing, about 4 us, to each graph replay.)"""
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
         for i in range(steps):
-            evs[i][0].record(stream)
             fn(i)
-            evs[i][1].record(stream)
+        e1.record(stream)
         stream.synchronize()
-        return [a.elapsed_time(b) for a, b in evs]
+        return [e0.elapsed_time(e1) / steps] * steps
 
     # ---- batched (value) ----
     # clocks are sampled over a load window: >= 1.5 s of back-to-back warm-up
@@ -522,19 +525,32 @@ def run_frg(args):
     plain_value = n / (statistics.mean(plain_ms) * 1e-3)
 
     # ---- e2e through the C ABI with host buffers ----
-    hq, hqd, hu = (frg.lib().frg_host_alloc(7 * 4 * n) for _ in range(3))
-    hout = [frg.lib().frg_host_alloc(w * 4 * n) for w in (98, 7, 49)]
-    for ptr, arr in ((hq, q), (hqd, qd), (hu, u)):
-        np.ctypeslib.as_array((ctypes.c_float * (7 * n)).from_address(ptr))[:] = arr.reshape(-1)
-    for _ in range(max(1, args.warmup)):
-        ctx.gradient_host_into(n, hq, hqd, hu, *hout)
+    # two sets of pinned buffers: the pipelined call keeps two batches in
+    # flight, and neighbouring batches must not share output arrays
+    hsets = []
+    for _ in range(2):
+        hin = [frg.lib().frg_host_alloc(7 * 4 * n) for _ in range(3)]
+        hout = [frg.lib().frg_host_alloc(w * 4 * n) for w in (98, 7, 49)]
+        for ptr, arr in zip(hin, (q, qd, u)):
+            np.ctypeslib.as_array((ctypes.c_float * (7 * n)).from_address(ptr))[:] = arr.reshape(-1)
+        hsets.append(hin + hout)
     e2e_steps = max(5, args.steps // 5)
+    # one frg_gradient_host call per step (synchronous: launch, results, return)
+    for _ in range(max(1, args.warmup)):
+        ctx.gradient_host_into(n, *hsets[0])
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        ctx.gradient_host_into(n, hq, hqd, hu, *hout)
+        ctx.gradient_host_into(n, *hsets[0])
+    e2e_single_s = (time.perf_counter() - t0) / e2e_steps
+    # the same steps as batches of one frg_gradient_host_batches call
+    batches = [(n, *hsets[i % 2]) for i in range(e2e_steps)]
+    ctx.gradient_host_batches(batches[:max(2, args.warmup)])
+    t0 = time.perf_counter()
+    ctx.gradient_host_batches(batches)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    for p in [hq, hqd, hu] + hout:
-        frg.lib().frg_host_free(p)
+    for hs in hsets:
+        for p in hs:
+            frg.lib().frg_host_free(p)
 
     link = host_link_rates(torch, dev, stream, 616 * n)
 
@@ -575,10 +591,15 @@ def run_frg(args):
                 "autotune_knots_per_s": tuned, "parallelism": f"replicas x{ws} (knots sharded, no collective)",
             },
             "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 84 * n, "d2h_bytes_per_step": 616 * n,
-                    "call": "frg_gradient_host (pinned host buffers)", "ms_per_step": e2e_s * 1e3,
+                    "call": f"frg_gradient_host_batches: {e2e_steps} steps, each the whole mix from pinned host "
+                            f"buffers to pinned host buffers, two batches in flight",
+                    "ms_per_step": e2e_s * 1e3,
                     "host_link": dict(link, bound="d2h: results' bytes / measured device-to-host copy rate",
                                       bound_ms=d2h_s * 1e3),
-                    "host_link_frac": d2h_s / e2e_s},
+                    "host_link_frac": d2h_s / e2e_s,
+                    "single_call": {"value": n / e2e_single_s, "ms_per_step": e2e_single_s * 1e3,
+                                    "host_link_frac": d2h_s / e2e_single_s,
+                                    "call": "one synchronous frg_gradient_host per step"}},
             "plain_per_trajectory": {"value": plain_value, "unit": UNIT, "launches_per_step": n_traj,
                                      "ms_per_step": statistics.mean(plain_ms)},
             "batched_vs_plain": value / ws / plain_value,

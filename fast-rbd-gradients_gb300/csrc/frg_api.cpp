@@ -216,6 +216,7 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
         !check(ctx, frg::init_ext_kernels(), "fext / forward-dynamics kernel set-up") ||
         !check(ctx, frg::init_f64_kernels(), "FP64 kernel set-up") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream2, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !check(ctx, cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming), "cudaEventCreate")) {
         g_orphan_error = ctx->err;
         frg_destroy(ctx);
@@ -236,11 +237,14 @@ void frg_destroy(frg_ctx *ctx) {
     {
         DeviceGuard g(ctx->device);
         if (ctx->io_stream) cudaStreamSynchronize(ctx->io_stream);
+        if (ctx->io_stream2) cudaStreamSynchronize(ctx->io_stream2);
         if (ctx->scratch_done) cudaEventSynchronize(ctx->scratch_done);
         ctx->scratch.release();
         cudaFree(ctx->host_buf);
+        cudaFree(ctx->host_buf2);
         cudaFree(ctx->f64_buf);
         if (ctx->io_stream) cudaStreamDestroy(ctx->io_stream);
+        if (ctx->io_stream2) cudaStreamDestroy(ctx->io_stream2);
         if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
     }
     delete ctx;
@@ -456,6 +460,23 @@ frg_status frg_verify_f64(frg_ctx *ctx, int n_knots, const float *q, const float
 
 namespace {
 
+// Grows a ctx-owned device buffer to `need` floats (cudaFree waits for earlier
+// work that may still use it).
+bool ensure_floats(frg_ctx *ctx, float **buf, size_t *cap, size_t need, const char *who) {
+    if (need <= *cap) return true;
+    cudaFree(*buf);
+    *buf = nullptr;
+    *cap = 0;
+    if (cudaMalloc(buf, need * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        *buf = nullptr;
+        frg_set_error(ctx, std::string(who) + ": cudaMalloc of " + std::to_string(need * 4) + " bytes failed");
+        return false;
+    }
+    *cap = need;
+    return true;
+}
+
 // True if the GPU of ctx can load/store `p` directly: pinned (page-locked,
 // mapped) host memory, or device memory.
 bool device_accessible(const void *p) {
@@ -535,6 +556,64 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
         !check(ctx, cudaMemcpyAsync(qdd, dqdd_, b7, cudaMemcpyDeviceToHost, s), "D2H qdd") ||
         !check(ctx, cudaMemcpyAsync(minv, dminv, frg::kMinvN * n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H minv") ||
         !check(ctx, cudaStreamSynchronize(s), "frg_gradient_host sync"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+frg_status frg_gradient_host_batches(frg_ctx *ctx, int n_batches, const frg_host_batch *batches) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_batches < 0 || (n_batches > 0 && !batches)) {
+        frg_set_error(ctx, "frg_gradient_host_batches: bad batch list");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    bool pinned = true;
+    size_t max_n = 0;
+    for (int i = 0; i < n_batches; i++) {
+        const frg_host_batch &b = batches[i];
+        if (b.n_knots < 0 || (b.n_knots > 0 && !(b.q && b.qd && b.u && b.dqdd && b.qdd && b.minv))) {
+            frg_set_error(ctx, "frg_gradient_host_batches: batch " + std::to_string(i) + ": negative size or null pointer");
+            return FRG_ERR_INVALID_ARGUMENT;
+        }
+        if (b.n_knots == 0) continue;
+        max_n = std::max(max_n, static_cast<size_t>(b.n_knots));
+        pinned = pinned && device_accessible(b.q) && device_accessible(b.qd) && device_accessible(b.u) &&
+                 device_accessible(b.dqdd) && device_accessible(b.qdd) && device_accessible(b.minv);
+    }
+    if (!pinned) {  // pageable arrays: one staged call after the other
+        for (int i = 0; i < n_batches; i++) {
+            const frg_host_batch &b = batches[i];
+            const frg_status st = frg_gradient_host(ctx, b.n_knots, b.q, b.qd, b.u, b.dqdd, b.qdd, b.minv);
+            if (st != FRG_OK) return st;
+        }
+        return FRG_OK;
+    }
+    if (max_n == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    const size_t need = frg::kDqddN * max_n;
+    if (!ensure_floats(ctx, &ctx->host_buf, &ctx->host_buf_floats, need, "frg_gradient_host_batches") ||
+        !ensure_floats(ctx, &ctx->host_buf2, &ctx->host_buf2_floats, need, "frg_gradient_host_batches"))
+        return FRG_ERR_OUT_OF_MEMORY;
+    // Batches alternate between two streams, each with its own dqdd relay
+    // buffer, so two launches are in flight at once: one batch's launch and
+    // first tiles (before any result exists) overlap the previous batch's
+    // results streaming over the host link.  A batch reuses its stream's relay
+    // buffer only after the batch two places before it, in stream order.
+    for (int i = 0; i < n_batches; i++) {
+        const frg_host_batch &b = batches[i];
+        if (b.n_knots == 0) continue;
+        const bool odd = (i & 1) != 0;
+        if (!check(ctx,
+                   frg::launch_host_out(ctx->damping, ctx->mpc, ctx->shape, b.n_knots, b.q, b.qd, b.u,
+                                        odd ? ctx->host_buf2 : ctx->host_buf, b.dqdd, b.qdd, b.minv,
+                                        odd ? ctx->io_stream2 : ctx->io_stream),
+                   "frg_gradient_host_batches launch")) {
+            cudaStreamSynchronize(ctx->io_stream);
+            cudaStreamSynchronize(ctx->io_stream2);
+            return FRG_ERR_CUDA;
+        }
+    }
+    const cudaError_t e1 = cudaStreamSynchronize(ctx->io_stream), e2 = cudaStreamSynchronize(ctx->io_stream2);
+    if (!check(ctx, e1, "frg_gradient_host_batches sync") || !check(ctx, e2, "frg_gradient_host_batches sync"))
         return FRG_ERR_CUDA;
     return FRG_OK;
 }

@@ -54,6 +54,9 @@ struct frg_ctx {
     cudaStream_t io_stream = nullptr;   // frg_gradient_host
     float *host_buf = nullptr;          // device staging for frg_gradient_host (dqdd relay / pageable path)
     size_t host_buf_floats = 0;
+    cudaStream_t io_stream2 = nullptr;  // frg_gradient_host_batches: odd batches
+    float *host_buf2 = nullptr;         // their dqdd relay
+    size_t host_buf2_floats = 0;
     DeviceBatch scratch;                // frg_gradient_batched descriptors
     double *f64_buf = nullptr;          // frg_verify_f64 scratch (frg::kSlotN doubles per knot)
     size_t f64_buf_doubles = 0;

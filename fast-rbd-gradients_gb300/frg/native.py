@@ -38,7 +38,7 @@ EXPORTED = (
     "frg_forward_dynamics", "frg_discrete_jacobians", "frg_gradient_f64", "frg_verify_f64", "frg_get_tuning",
     "frg_set_tuning", "frg_knot_status", "frg_model_name", "frg_gradient_knots", "frg_server_cancel",
     "frg_single_knot_latency", "frg_server_submit_device", "frg_server_submit_resident", "frg_server_slot",
-    "frg_model_dofs",
+    "frg_model_dofs", "frg_gradient_host_batches",
 )
 SERVE_HOST_RESULTS = 1
 
@@ -61,6 +61,11 @@ class Traj(ctypes.Structure):
     _fields_ = [("n_knots", ctypes.c_int64), ("q", ctypes.c_void_p), ("qd", ctypes.c_void_p),
                 ("u", ctypes.c_void_p), ("dqdd", ctypes.c_void_p), ("qdd", ctypes.c_void_p),
                 ("minv", ctypes.c_void_p)]
+
+
+class HostBatch(ctypes.Structure):
+    _fields_ = [("n_knots", ctypes.c_int), ("q", ctypes.c_void_p), ("qd", ctypes.c_void_p), ("u", ctypes.c_void_p),
+                ("dqdd", ctypes.c_void_p), ("qdd", ctypes.c_void_p), ("minv", ctypes.c_void_p)]
 
 
 class Tuning(ctypes.Structure):
@@ -154,6 +159,7 @@ def _declare(L):
         "frg_server_submit_resident": (st, [vp, ctypes.c_uint64, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint64)]),
         "frg_server_slot": (st, [vp, ctypes.c_uint64, ctypes.POINTER(SlotInfo)]),
         "frg_model_dofs": (i32, []),
+        "frg_gradient_host_batches": (st, [vp, i32, ctypes.POINTER(HostBatch)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -372,6 +378,14 @@ class Context:
         """Host-buffer path: inputs in, outputs written to the given host arrays."""
         self._check(lib().frg_gradient_host(self._h, int(n_knots), _ptr(q), _ptr(qd), _ptr(u), _ptr(dqdd),
                                             _ptr(qdd), _ptr(minv)), "frg_gradient_host")
+
+    def gradient_host_batches(self, batches):
+        """Host-buffer batches in one call: each (n, q, qd, u, dqdd, qdd, minv)
+        with host arrays or addresses; two launches kept in flight."""
+        arr = (HostBatch * max(1, len(batches)))()
+        for i, (n, *ptrs) in enumerate(batches):
+            arr[i] = HostBatch(int(n), *[_ptr(p) for p in ptrs])
+        self._check(lib().frg_gradient_host_batches(self._h, len(batches), arr), "frg_gradient_host_batches")
 
     def gradient_host(self, q, qd, u):
         """numpy float32 [n,N] x3 -> (dqdd [n,2N^2], qdd [n,N], minv [n,N^2])."""

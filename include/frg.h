@@ -148,6 +148,25 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
                              float *dqdd, float *qdd, float *minv);
 
 /*
+ * Many host-buffer batches in one call (a caller streaming batch after batch
+ * through host memory): each batch as frg_gradient_host, returning when every
+ * result is in its host arrays.  With pinned arrays the batches alternate
+ * between two internal streams, two launches in flight at once, so a batch's
+ * launch and first tiles -- about 25 us in which no result exists yet -- overlap
+ * the previous batch's results streaming over the host link, which then stays
+ * busy.  Batches must not share output arrays with other batches of the call
+ * that may be in flight (neighbouring ones).  Pageable arrays are processed one
+ * batch after the other.  No counterpart in the reference, whose
+ * time_GPU.cu:310-330 loop synchronises after every batch.
+ */
+typedef struct frg_host_batch {
+    int n_knots;
+    const float *q, *qd, *u;
+    float *dqdd, *qdd, *minv;
+} frg_host_batch;
+frg_status frg_gradient_host_batches(frg_ctx *ctx, int n_batches, const frg_host_batch *batches);
+
+/*
  * The reference's own per-knot layout, for callers that already pack it: the
  * knot<T> record of helpers_CPU/dynamicsGradient.h:19-25, [q N | qd N | u N |
  * qdd N | Minv N^2] = FRG_KNOT_RECORD_FLOATS (4N + N^2) floats per knot, as time_GPU.cu:
