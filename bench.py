@@ -8,9 +8,12 @@ through the full path (RNEA, Minv, q̈, dtau/dq, dtau/dqd, -Minv dtau) in FP32.
   value     knot-gradients/s of the batched form: one persistent launch over
             the ragged offset list, replayed as a CUDA graph, inputs resident
             in HBM; 6 rotating input/output sets (~280 MB > 129 MB L2).
-  e2e       the same metric through the C ABI's host-buffer call
-            (frg_gradient_host): H2D of q, qd, u from pinned memory, kernel,
-            D2H of dqdd, qdd, Minv inside every timed step.
+  e2e       the same metric through the C ABI's host-buffer calls: H2D of
+            q, qd, u from pinned memory, kernel, D2H of dqdd, qdd, Minv
+            inside every timed step (frg_gradient_host_batches, two steps in
+            flight; e2e.single_call: one synchronous frg_gradient_host per
+            step; e2e.gradient_only: dqdd alone returned, as the reference's
+            Completely Fused call returns it).
   plain     the plain form of the same mix: one launch per trajectory.
   plain_scaling  one plain launch per batch of N contiguous knots, N in
             {16, 32, 64, 128, 1024, 65536} (L2 warm), plus N = 1 (single-knot
@@ -548,6 +551,13 @@ def run_frg(args):
     t0 = time.perf_counter()
     ctx.gradient_host_batches(batches)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
+    # the reference's "Completely Fused" output (time_GPU.cu:316 copies back
+    # dqdd only): q̈ and Minv not asked for, so they stay on the device
+    grad_only = [(n, *hsets[i % 2][:4], None, None) for i in range(e2e_steps)]
+    ctx.gradient_host_batches(grad_only[:max(2, args.warmup)])
+    t0 = time.perf_counter()
+    ctx.gradient_host_batches(grad_only)
+    e2e_grad_s = (time.perf_counter() - t0) / e2e_steps
     for hs in hsets:
         for p in hs:
             frg.lib().frg_host_free(p)
@@ -599,7 +609,12 @@ def run_frg(args):
                     "host_link_frac": d2h_s / e2e_s,
                     "single_call": {"value": n / e2e_single_s, "ms_per_step": e2e_single_s * 1e3,
                                     "host_link_frac": d2h_s / e2e_single_s,
-                                    "call": "one synchronous frg_gradient_host per step"}},
+                                    "call": "one synchronous frg_gradient_host per step"},
+                    "gradient_only": {"value": n / e2e_grad_s, "ms_per_step": e2e_grad_s * 1e3,
+                                      "d2h_bytes_per_step": 392 * n,
+                                      "host_link_frac": d2h_s * 392 / 616 / e2e_grad_s,
+                                      "call": "frg_gradient_host_batches with qdd and minv NULL: dqdd alone "
+                                              "returned, the output of the reference's Completely Fused call"}},
             "plain_per_trajectory": {"value": plain_value, "unit": UNIT, "launches_per_step": n_traj,
                                      "ms_per_step": statistics.mean(plain_ms)},
             "batched_vs_plain": value / ws / plain_value,

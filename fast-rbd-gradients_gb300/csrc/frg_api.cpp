@@ -489,12 +489,32 @@ bool device_accessible(const void *p) {
            a.type == cudaMemoryTypeManaged;
 }
 
+// Results a host call returns: dqdd always; q̈ and Minv unless their host
+// array is NULL.  The kernel still writes a result that is not asked for --
+// into the tail of the ctx-owned relay buffer, [dqdd | q̈ | Minv], so in device
+// memory -- and no byte of it crosses the host link.
+struct HostOuts {
+    float *dqdd, *qdd, *minv;
+};
+
+size_t relay_floats(size_t n, const float *qdd, const float *minv) {
+    if (!minv) return (frg::kDqddN + frg::kN + frg::kMinvN) * n;
+    if (!qdd) return (frg::kDqddN + frg::kN) * n;
+    return frg::kDqddN * n;
+}
+
+HostOuts host_outs(float *relay, size_t n, float *qdd, float *minv) {
+    return HostOuts{relay, qdd ? qdd : relay + frg::kDqddN * n, minv ? minv : relay + (frg::kDqddN + frg::kN) * n};
+}
+
+bool host_or_null_accessible(const void *p) { return !p || device_accessible(p); }
+
 }  // namespace
 
 frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
                              float *dqdd, float *qdd, float *minv) {
     if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
-    if (n_knots < 0 || (n_knots > 0 && !(q && qd && u && dqdd && qdd && minv))) {
+    if (n_knots < 0 || (n_knots > 0 && !(q && qd && u && dqdd))) {
         frg_set_error(ctx, "frg_gradient_host: negative n_knots or null pointer");
         return FRG_ERR_INVALID_ARGUMENT;
     }
@@ -509,40 +529,22 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
     // The results stream out while later tiles compute, so the host link's
     // device-to-host rate (about 190 GB/s here) bounds the call.
     if (device_accessible(q) && device_accessible(qd) && device_accessible(u) && device_accessible(dqdd) &&
-        device_accessible(qdd) && device_accessible(minv)) {
-        const size_t need = frg::kDqddN * n;
-        if (need > ctx->host_buf_floats) {
-            cudaFree(ctx->host_buf);
-            ctx->host_buf = nullptr;
-            ctx->host_buf_floats = 0;
-            if (cudaMalloc(&ctx->host_buf, need * sizeof(float)) != cudaSuccess) {
-                cudaGetLastError();
-                frg_set_error(ctx, "frg_gradient_host: cudaMalloc of " + std::to_string(need * 4) + " bytes failed");
-                return FRG_ERR_OUT_OF_MEMORY;
-            }
-            ctx->host_buf_floats = need;
-        }
+        host_or_null_accessible(qdd) && host_or_null_accessible(minv)) {
+        if (!ensure_floats(ctx, &ctx->host_buf, &ctx->host_buf_floats, relay_floats(n, qdd, minv),
+                           "frg_gradient_host"))
+            return FRG_ERR_OUT_OF_MEMORY;
+        const HostOuts o = host_outs(ctx->host_buf, n, qdd, minv);
         if (!check(ctx,
-                   frg::launch_host_out(ctx->damping, ctx->mpc, ctx->shape, n_knots, q, qd, u, ctx->host_buf, dqdd,
-                                        qdd, minv, s),
+                   frg::launch_host_out(ctx->damping, ctx->mpc, ctx->shape, n_knots, q, qd, u, o.dqdd, dqdd, o.qdd,
+                                        o.minv, s),
                    "frg_gradient_host launch") ||
             !check(ctx, cudaStreamSynchronize(s), "frg_gradient_host sync"))
             return FRG_ERR_CUDA;
         return FRG_OK;
     }
     // Pageable host arrays: stage through device buffers owned by ctx.
-    const size_t need = n * frg::kSlotN;
-    if (need > ctx->host_buf_floats) {
-        cudaFree(ctx->host_buf);
-        ctx->host_buf = nullptr;
-        ctx->host_buf_floats = 0;
-        if (cudaMalloc(&ctx->host_buf, need * sizeof(float)) != cudaSuccess) {
-            cudaGetLastError();
-            frg_set_error(ctx, "frg_gradient_host: cudaMalloc of " + std::to_string(need * 4) + " bytes failed");
-            return FRG_ERR_OUT_OF_MEMORY;
-        }
-        ctx->host_buf_floats = need;
-    }
+    if (!ensure_floats(ctx, &ctx->host_buf, &ctx->host_buf_floats, n * frg::kSlotN, "frg_gradient_host"))
+        return FRG_ERR_OUT_OF_MEMORY;
     float *b = ctx->host_buf;
     float *dq = b, *dqd = b + frg::kSlotQd * n, *du = b + frg::kSlotU * n, *ddqdd = b + frg::kSlotDqdd * n,
           *dqdd_ = b + frg::kSlotQdd * n, *dminv = b + frg::kSlotMinv * n;
@@ -553,8 +555,10 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
         !check(ctx, frg::launch_plain(ctx->damping, ctx->mpc, ctx->shape, n_knots, dq, dqd, du, ddqdd, dqdd_, dminv, s),
                "frg_gradient_host launch") ||
         !check(ctx, cudaMemcpyAsync(dqdd, ddqdd, frg::kDqddN * n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H dqdd") ||
-        !check(ctx, cudaMemcpyAsync(qdd, dqdd_, b7, cudaMemcpyDeviceToHost, s), "D2H qdd") ||
-        !check(ctx, cudaMemcpyAsync(minv, dminv, frg::kMinvN * n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H minv") ||
+        (qdd && !check(ctx, cudaMemcpyAsync(qdd, dqdd_, b7, cudaMemcpyDeviceToHost, s), "D2H qdd")) ||
+        (minv &&
+         !check(ctx, cudaMemcpyAsync(minv, dminv, frg::kMinvN * n * sizeof(float), cudaMemcpyDeviceToHost, s),
+                "D2H minv")) ||
         !check(ctx, cudaStreamSynchronize(s), "frg_gradient_host sync"))
         return FRG_ERR_CUDA;
     return FRG_OK;
@@ -567,17 +571,17 @@ frg_status frg_gradient_host_batches(frg_ctx *ctx, int n_batches, const frg_host
         return FRG_ERR_INVALID_ARGUMENT;
     }
     bool pinned = true;
-    size_t max_n = 0;
+    size_t need = 0;
     for (int i = 0; i < n_batches; i++) {
         const frg_host_batch &b = batches[i];
-        if (b.n_knots < 0 || (b.n_knots > 0 && !(b.q && b.qd && b.u && b.dqdd && b.qdd && b.minv))) {
+        if (b.n_knots < 0 || (b.n_knots > 0 && !(b.q && b.qd && b.u && b.dqdd))) {
             frg_set_error(ctx, "frg_gradient_host_batches: batch " + std::to_string(i) + ": negative size or null pointer");
             return FRG_ERR_INVALID_ARGUMENT;
         }
         if (b.n_knots == 0) continue;
-        max_n = std::max(max_n, static_cast<size_t>(b.n_knots));
+        need = std::max(need, relay_floats(static_cast<size_t>(b.n_knots), b.qdd, b.minv));
         pinned = pinned && device_accessible(b.q) && device_accessible(b.qd) && device_accessible(b.u) &&
-                 device_accessible(b.dqdd) && device_accessible(b.qdd) && device_accessible(b.minv);
+                 device_accessible(b.dqdd) && host_or_null_accessible(b.qdd) && host_or_null_accessible(b.minv);
     }
     if (!pinned) {  // pageable arrays: one staged call after the other
         for (int i = 0; i < n_batches; i++) {
@@ -587,9 +591,8 @@ frg_status frg_gradient_host_batches(frg_ctx *ctx, int n_batches, const frg_host
         }
         return FRG_OK;
     }
-    if (max_n == 0) return FRG_OK;
+    if (need == 0) return FRG_OK;
     DeviceGuard g(ctx->device);
-    const size_t need = frg::kDqddN * max_n;
     if (!ensure_floats(ctx, &ctx->host_buf, &ctx->host_buf_floats, need, "frg_gradient_host_batches") ||
         !ensure_floats(ctx, &ctx->host_buf2, &ctx->host_buf2_floats, need, "frg_gradient_host_batches"))
         return FRG_ERR_OUT_OF_MEMORY;
@@ -602,10 +605,11 @@ frg_status frg_gradient_host_batches(frg_ctx *ctx, int n_batches, const frg_host
         const frg_host_batch &b = batches[i];
         if (b.n_knots == 0) continue;
         const bool odd = (i & 1) != 0;
+        const HostOuts o = host_outs(odd ? ctx->host_buf2 : ctx->host_buf, static_cast<size_t>(b.n_knots), b.qdd,
+                                     b.minv);
         if (!check(ctx,
-                   frg::launch_host_out(ctx->damping, ctx->mpc, ctx->shape, b.n_knots, b.q, b.qd, b.u,
-                                        odd ? ctx->host_buf2 : ctx->host_buf, b.dqdd, b.qdd, b.minv,
-                                        odd ? ctx->io_stream2 : ctx->io_stream),
+                   frg::launch_host_out(ctx->damping, ctx->mpc, ctx->shape, b.n_knots, b.q, b.qd, b.u, o.dqdd, b.dqdd,
+                                        o.qdd, o.minv, odd ? ctx->io_stream2 : ctx->io_stream),
                    "frg_gradient_host_batches launch")) {
             cudaStreamSynchronize(ctx->io_stream);
             cudaStreamSynchronize(ctx->io_stream2);

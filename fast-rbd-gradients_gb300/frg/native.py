@@ -387,15 +387,16 @@ class Context:
             arr[i] = HostBatch(int(n), *[_ptr(p) for p in ptrs])
         self._check(lib().frg_gradient_host_batches(self._h, len(batches), arr), "frg_gradient_host_batches")
 
-    def gradient_host(self, q, qd, u):
-        """numpy float32 [n,N] x3 -> (dqdd [n,2N^2], qdd [n,N], minv [n,N^2])."""
+    def gradient_host(self, q, qd, u, want_qdd=True, want_minv=True):
+        """numpy float32 [n,N] x3 -> (dqdd [n,2N^2], qdd [n,N], minv [n,N^2]);
+        a result not wanted is None and is not copied back."""
         import numpy as np
         q, qd, u = (np.ascontiguousarray(x, dtype=np.float32) for x in (q, qd, u))
         n = q.shape[0]
         nj, nd, nm = dims()
         dqdd = np.empty((n, nd), np.float32)
-        qdd = np.empty((n, nj), np.float32)
-        minv = np.empty((n, nm), np.float32)
+        qdd = np.empty((n, nj), np.float32) if want_qdd else None
+        minv = np.empty((n, nm), np.float32) if want_minv else None
         self.gradient_host_into(n, q, qd, u, dqdd, qdd, minv)
         return dqdd, qdd, minv
 

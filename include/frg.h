@@ -143,6 +143,12 @@ frg_status frg_single_knot_latency(frg_ctx *ctx, int lanes_per_knot, int iters, 
  * writes each 32-knot tile's results to the host arrays as soon as the tile
  * finishes, so the transfer overlaps the arithmetic.  Pageable arrays are
  * staged through device buffers owned by ctx.
+ *
+ * qdd and/or minv may be NULL: that result is then not returned, and none of
+ * its bytes cross the host link (the kernel writes it to device memory owned by
+ * ctx).  dqdd alone is what the reference's "Completely Fused" call returns
+ * (time_GPU.cu:316 copies back d_dqdd only): 392 of the 616 result bytes per
+ * knot at 7 joints.
  */
 frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
                              float *dqdd, float *qdd, float *minv);
@@ -155,7 +161,8 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
  * launch and first tiles -- about 25 us in which no result exists yet -- overlap
  * the previous batch's results streaming over the host link, which then stays
  * busy.  Batches must not share output arrays with other batches of the call
- * that may be in flight (neighbouring ones).  Pageable arrays are processed one
+ * that may be in flight (neighbouring ones).  A batch's qdd and minv may be
+ * NULL, as in frg_gradient_host.  Pageable arrays are processed one
  * batch after the other.  No counterpart in the reference, whose
  * time_GPU.cu:310-330 loop synchronises after every batch.
  */

@@ -63,3 +63,54 @@ def test_batches_reject_null_arrays():
         with pytest.raises(frg.FrgError):
             ctx.gradient_host_batches([(10, None, None, None, None, None, None)])
         ctx.gradient_host_batches([])  # nothing to do
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+@pytest.mark.parametrize("lanes", [1, 8])
+def test_results_not_asked_for_are_not_returned(pinned, lanes):
+    """qdd and/or minv NULL: dqdd (and the other result asked for) carry the
+    bits of the full call, in single calls and in batches."""
+    sizes = [900, 31, 2049, 5]
+    keep = [(True, False), (False, True), (False, False), (True, True)]  # (qdd, minv)
+    data = [frg.sample_knots(n, seed=80 + i) for i, n in enumerate(sizes)]
+    owned = []
+
+    def arr(shape, fill=None):
+        if pinned:
+            p, a = _pinned(shape)
+            owned.append(p)
+        else:
+            a = np.empty(shape, np.float32)
+        if fill is not None:
+            a[:] = fill
+        return a
+
+    try:
+        with frg.Context() as ctx:
+            ctx.set_lanes_per_knot(lanes)
+            want = [ctx.gradient_host(q, qd, u) for q, qd, u in data]
+            batches, outs = [], []
+            for (q, qd, u), n, (kq, km) in zip(data, sizes, keep):
+                ins = [arr(x.shape, x) for x in (q, qd, u)]
+                o = [arr((n, 98), np.nan), arr((n, 7), np.nan) if kq else None, arr((n, 49), np.nan) if km else None]
+                batches.append((n, *ins, *o))
+                outs.append(o)
+            ctx.gradient_host_batches(batches)
+            for o, w in zip(outs, want):
+                for a, b in zip(o, w):
+                    if a is not None:
+                        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+            for (n, *ins, _, _, _), (kq, km), w in zip(batches, keep, want):
+                o = [arr((n, 98), np.nan), arr((n, 7), np.nan) if kq else None, arr((n, 49), np.nan) if km else None]
+                ctx.gradient_host_into(n, *ins, *o)
+                for a, b in zip(o, w):
+                    if a is not None:
+                        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+            d, qdd, minv = ctx.gradient_host(*data[0], want_qdd=False, want_minv=False)
+            assert qdd is None and minv is None
+            assert np.array_equal(d.view(np.uint32), want[0][0].view(np.uint32))
+            with pytest.raises(frg.FrgError):  # dqdd is always returned
+                ctx.gradient_host_into(5, *data[3], None, None, None)
+    finally:
+        for p in owned:
+            native.lib().frg_host_free(p)
