@@ -113,15 +113,13 @@ __device__ __forceinline__ bool aligned16(const void *p) {
 }
 
 // Element e = lane + 32 m (m < W) of a tile's W reals per knot is entry
-// e % W of knot e / W; step (kn, j) from element e to e + 32.
+// j = e % W of knot kn = e / W.  Computed afresh for every element (a
+// multiply-high by a constant, independent across elements) rather than
+// stepped from the previous one, whose serial chain of adds and compares
+// held each store or load back by the one before.
 template <int W>
-__device__ __forceinline__ void next_element(int &kn, int &j) {
-    kn += 32 / W;
-    j += 32 % W;
-    if (j >= W) {
-        j -= W;
-        kn++;
-    }
+__device__ __forceinline__ int element_knot(int e) {
+    return static_cast<int>(static_cast<unsigned int>(e) / W);
 }
 
 // Gather of W reals per knot (knot-major) into stage[lane*W + j].  Tiles of
@@ -150,13 +148,12 @@ __device__ __forceinline__ void gather_in(real *stage, const real *base, int lan
     if constexpr (W <= 8) {
         knot[lane] = base;
         __syncwarp();
-        int kn = lane / W, j = lane % W;
         const real *p[W];
 #pragma unroll
         for (int m = 0; m < W; m++) {
+            const int e = lane + 32 * m, kn = element_knot<W>(e);
             p[m] = knot[kn];
-            if (p[m]) p[m] += j;
-            next_element<W>(kn, j);
+            if (p[m]) p[m] += e - kn * W;
         }
         real v[W];
 #pragma unroll
@@ -200,11 +197,10 @@ __device__ __forceinline__ void scatter_out(const real *stage, real *base, int l
                     if (e < lim) b0[e] = stage[e];
             }
         } else {
-            int kn = lane / W, j = lane % W;
 #pragma unroll 7
-            for (int e = lane; e < 32 * W; e += 32) {
-                if (kn < n) b0[kn * STRIDE + j] = stage[e];
-                next_element<W>(kn, j);
+            for (int m = 0; m < W; m++) {
+                const int e = lane + 32 * m, kn = element_knot<W>(e);
+                if (kn < n) b0[e + kn * (STRIDE - W)] = stage[e];
             }
         }
     } else {
@@ -212,17 +208,16 @@ __device__ __forceinline__ void scatter_out(const real *stage, real *base, int l
         static_assert(W % G == 0, "split-tile stores go in groups of kJoints");
         knot[lane] = base;
         __syncwarp();
-        int kn = lane / W, j = lane % W;
 #pragma unroll 1
         for (int m0 = 0; m0 < W; m0 += G) {
             real *p[G];
             real v[G];
 #pragma unroll
             for (int i = 0; i < G; i++) {
+                const int e = lane + 32 * (m0 + i), kn = element_knot<W>(e);
                 p[i] = const_cast<real *>(knot[kn]);
-                if (p[i]) p[i] += j;
-                v[i] = stage[lane + 32 * (m0 + i)];
-                next_element<W>(kn, j);
+                if (p[i]) p[i] += e - kn * W;
+                v[i] = stage[e];
             }
 #pragma unroll
             for (int i = 0; i < G; i++)
