@@ -269,9 +269,9 @@ frg_status frg_gradient_ragged(frg_ctx *ctx, int n_traj, const int64_t *offsets,
  * that every GPU loading the library holds until process exit, so at most
  * FRG_NOALLOC_MAX_TRAJ trajectories and FRG_NOALLOC_MAX_KNOTS knots per call
  * (larger batches return FRG_ERR_INVALID_ARGUMENT).  The first call on a
- * device looks up that array's device address on that device: make it
- * before any stream capture.  All calls share the array: calls whose launches
- * may overlap on the GPU (different streams, unordered) race -- order them.
+ * device looks up that array's device address on that device.  All calls
+ * share the array: calls whose launches may overlap on the GPU (different
+ * streams, unordered) race -- order them.
  */
 #define FRG_NOALLOC_MAX_TRAJ 4096
 #define FRG_NOALLOC_MAX_KNOTS (65536 * 32)
