@@ -185,14 +185,19 @@ frg_status frg_autotune(frg_ctx *ctx, int64_t n_knots, double *best_knots_per_s)
             }
         }
     // 2) scattered trajectories: the persistent kernel (x resident CTAs per SM),
-    //    on the same knots cut into 128-knot trajectories in reversed order
+    //    on the same knots cut into trajectories of 8 to 256 knots (seeded),
+    //    listed in shuffled order: most tiles then span two trajectories stored
+    //    apart, as in a solver's batch.  (Whole-tile trajectories favour shapes
+    //    with fewer resident warps that lose on such batches.)
     std::vector<frg_traj> scattered;
-    for (size_t k0 = 0; k0 < n; k0 += 128) {
-        const size_t m = std::min<size_t>(128, n - k0);
+    std::uniform_int_distribution<int> uh(8, 256);
+    for (size_t k0 = 0; k0 < n;) {
+        const size_t m = std::min<size_t>(static_cast<size_t>(uh(rng)), n - k0);
         scattered.push_back(frg_traj{static_cast<int64_t>(m), tr.q + kN * k0, tr.qd + kN * k0, tr.u + kN * k0,
                                      tr.dqdd + frg::kDqddN * k0, tr.qdd + kN * k0, tr.minv + frg::kMinvN * k0});
+        k0 += m;
     }
-    std::reverse(scattered.begin(), scattered.end());
+    std::shuffle(scattered.begin(), scattered.end(), rng);
     HostBatch hs;
     DeviceBatch ds;
     good = good && frg_build_batch(static_cast<int>(scattered.size()), scattered.data(), hs, err) &&

@@ -286,7 +286,8 @@ class Context:
 
     def _check(self, st, what):
         if st != FRG_OK:
-            raise FrgError(st, f"{what}: {lib().frg_last_error(self._h).decode()}")
+            msg = lib().frg_last_error(self._h).decode()
+            raise FrgError(st, msg if msg.startswith(what) else f"{what}: {msg}")
 
     def last_error(self):
         return lib().frg_last_error(self._h).decode()
