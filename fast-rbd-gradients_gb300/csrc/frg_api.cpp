@@ -217,7 +217,10 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
         !check(ctx, frg::init_f64_kernels(), "FP64 kernel set-up") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream2, cudaStreamNonBlocking), "cudaStreamCreate") ||
-        !check(ctx, cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming), "cudaEventCreate")) {
+        !check(ctx, cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming), "cudaEventCreate") ||
+        !check(ctx, cudaEventCreateWithFlags(&ctx->batch_done[0], cudaEventDisableTiming), "cudaEventCreate") ||
+        !check(ctx, cudaEventCreateWithFlags(&ctx->batch_done[1], cudaEventDisableTiming), "cudaEventCreate") ||
+        !check(ctx, cudaEventCreateWithFlags(&ctx->batch_done[2], cudaEventDisableTiming), "cudaEventCreate")) {
         g_orphan_error = ctx->err;
         frg_destroy(ctx);
         return FRG_ERR_CUDA;
@@ -246,6 +249,10 @@ void frg_destroy(frg_ctx *ctx) {
         if (ctx->io_stream) cudaStreamDestroy(ctx->io_stream);
         if (ctx->io_stream2) cudaStreamDestroy(ctx->io_stream2);
         if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
+        for (cudaEvent_t e : ctx->batch_done)
+            if (e) cudaEventDestroy(e);
+        delete ctx->expander;  // joins its threads (no job is in flight between calls)
+        for (float *p : ctx->minv_stage) cudaFreeHost(p);
     }
     delete ctx;
 }
@@ -564,14 +571,92 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
     return FRG_OK;
 }
 
+namespace {
+
+// frg_gradient_host_batches when every batch returns Minv: Minv crosses the
+// host link as its packed upper triangle (kMinvPackedN instead of kMinvN
+// floats per knot: 532 instead of 616 result bytes per knot at 7 joints, and
+// the link bounds the call), into one of three pinned staging buffers; host
+// threads expand each batch to the caller's dense array while the next
+// batches compute and stream.  Expansions run one at a time, in batch order:
+// batch j - 1's starts when its launch has ended and batch j - 2's expansion
+// is done, right after batch j is launched; so batch j can reuse the staging
+// buffer of batch j - 3 without waiting, and two launches stay in flight.
+// Bits are those of the dense path (the expansion only copies).
+frg_status host_batches_packed(frg_ctx *ctx, int n_batches, const frg_host_batch *batches, size_t max_n) {
+    const size_t stage = static_cast<size_t>(frg::kMinvPackedN) * max_n;
+    if (ctx->minv_stage_floats < stage) {
+        for (float *&p : ctx->minv_stage) {
+            cudaFreeHost(p);  // waits for earlier work that may still write it
+            p = nullptr;
+        }
+        ctx->minv_stage_floats = 0;
+        for (float *&p : ctx->minv_stage)
+            if (cudaHostAlloc(reinterpret_cast<void **>(&p), stage * sizeof(float), cudaHostAllocPortable) !=
+                cudaSuccess) {
+                cudaGetLastError();
+                p = nullptr;
+                frg_set_error(ctx, "frg_gradient_host_batches: cudaHostAlloc of the Minv staging failed");
+                return FRG_ERR_OUT_OF_MEMORY;
+            }
+        ctx->minv_stage_floats = stage;
+    }
+    if (!ctx->expander) {
+        const unsigned hw = std::thread::hardware_concurrency();
+        // leave two cores to the calling thread and the CUDA driver
+        ctx->expander = new (std::nothrow) MinvExpander(static_cast<int>(std::min(14u, std::max(1u, hw > 2 ? hw - 2 : 1u))));
+        if (!ctx->expander) return FRG_ERR_OUT_OF_MEMORY;
+    }
+    MinvExpander &ex = *ctx->expander;
+    bool ok = true;
+    int j = 0, prev = -1;  // j: nonempty batches launched; prev: the last one
+    for (int i = 0; ok && i < n_batches; i++) {
+        const frg_host_batch &b = batches[i];
+        if (b.n_knots == 0) continue;
+        const int k = j % 3, odd = j & 1;
+        cudaStream_t st = odd ? ctx->io_stream2 : ctx->io_stream;
+        // dqdd relay per stream, and q̈ in the relay's tail when the caller does not want it
+        const HostOuts o = host_outs(odd ? ctx->host_buf2 : ctx->host_buf, static_cast<size_t>(b.n_knots), b.qdd,
+                                     b.minv);
+        ok = check(ctx,
+                   frg::launch_host_out(ctx->damping, ctx->mpc, ctx->shape, b.n_knots, b.q, b.qd, b.u, o.dqdd, b.dqdd,
+                                        o.qdd, ctx->minv_stage[k], st, true),
+                   "frg_gradient_host_batches launch") &&
+             check(ctx, cudaEventRecord(ctx->batch_done[k], st), "frg_gradient_host_batches");
+        if (ok && prev >= 0) {  // batch j - 1's launch has ended: expand it while batch j runs
+            const int kp = (j + 2) % 3;
+            ex.wait();  // batch j - 2's expansion
+            ok = check(ctx, cudaEventSynchronize(ctx->batch_done[kp]), "frg_gradient_host_batches sync");
+            if (ok) ex.start(ctx->minv_stage[kp], batches[prev].minv, static_cast<size_t>(batches[prev].n_knots));
+        }
+        prev = i;
+        j++;
+    }
+    if (ok && prev >= 0) {
+        const int kp = (j + 2) % 3;
+        ex.wait();
+        ok = check(ctx, cudaEventSynchronize(ctx->batch_done[kp]), "frg_gradient_host_batches sync");
+        if (ok) ex.start(ctx->minv_stage[kp], batches[prev].minv, static_cast<size_t>(batches[prev].n_knots));
+    }
+    ex.wait();
+    const cudaError_t e1 = cudaStreamSynchronize(ctx->io_stream), e2 = cudaStreamSynchronize(ctx->io_stream2);
+    if (!ok) return FRG_ERR_CUDA;
+    if (!check(ctx, e1, "frg_gradient_host_batches sync") || !check(ctx, e2, "frg_gradient_host_batches sync"))
+        return FRG_ERR_CUDA;
+    return FRG_OK;
+}
+
+}  // namespace
+
 frg_status frg_gradient_host_batches(frg_ctx *ctx, int n_batches, const frg_host_batch *batches) {
     if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
     if (n_batches < 0 || (n_batches > 0 && !batches)) {
         frg_set_error(ctx, "frg_gradient_host_batches: bad batch list");
         return FRG_ERR_INVALID_ARGUMENT;
     }
-    bool pinned = true;
-    size_t need = 0;
+    bool pinned = true, all_minv = true;
+    size_t need = 0, max_n = 0;
+    int nonempty = 0;
     for (int i = 0; i < n_batches; i++) {
         const frg_host_batch &b = batches[i];
         if (b.n_knots < 0 || (b.n_knots > 0 && !(b.q && b.qd && b.u && b.dqdd))) {
@@ -579,6 +664,9 @@ frg_status frg_gradient_host_batches(frg_ctx *ctx, int n_batches, const frg_host
             return FRG_ERR_INVALID_ARGUMENT;
         }
         if (b.n_knots == 0) continue;
+        nonempty++;
+        all_minv = all_minv && b.minv;
+        max_n = std::max(max_n, static_cast<size_t>(b.n_knots));
         need = std::max(need, relay_floats(static_cast<size_t>(b.n_knots), b.qdd, b.minv));
         pinned = pinned && device_accessible(b.q) && device_accessible(b.qd) && device_accessible(b.u) &&
                  device_accessible(b.dqdd) && host_or_null_accessible(b.qdd) && host_or_null_accessible(b.minv);
@@ -601,6 +689,8 @@ frg_status frg_gradient_host_batches(frg_ctx *ctx, int n_batches, const frg_host
     // first tiles (before any result exists) overlap the previous batch's
     // results streaming over the host link.  A batch reuses its stream's relay
     // buffer only after the batch two places before it, in stream order.
+    if (nonempty >= 2 && all_minv && ctx->shape.lanes_per_knot == 1)
+        return host_batches_packed(ctx, n_batches, batches, max_n);
     for (int i = 0; i < n_batches; i++) {
         const frg_host_batch &b = batches[i];
         if (b.n_knots == 0) continue;

@@ -15,6 +15,10 @@ namespace frg {
 
 constexpr int kN = FRG_MODEL_NUM_JOINTS;     // q, qd, u, qdd per knot
 constexpr int kMinvN = kN * kN;              // dense symmetric Minv
+// Minv's upper triangle, column by column (entries (r, c), r <= c), padded to
+// a multiple of N floats per knot: the form the pipelined host-buffer call
+// sends over the host link before expanding it to dense in host memory.
+constexpr int kMinvPackedN = kN * ((kN + 2) / 2);
 constexpr int kDqddN = 2 * kN * kN;          // [dqdd/dq | dqdd/dqd], N x 2N column-major
 constexpr int kFextN = 6 * kN;               // external spatial force per link
 constexpr int kRecordN = 4 * kN + kN * kN;   // the reference's knot record [q|qd|u|qdd|Minv]

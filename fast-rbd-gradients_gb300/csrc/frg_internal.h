@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "frg.h"
+#include "frg_expand.h"
 #include "frg_kernels.cuh"
 
 // Makes `device` current for a scope and restores the caller's device.
@@ -57,6 +58,13 @@ struct frg_ctx {
     cudaStream_t io_stream2 = nullptr;  // frg_gradient_host_batches: odd batches
     float *host_buf2 = nullptr;         // their dqdd relay
     size_t host_buf2_floats = 0;
+    // frg_gradient_host_batches: packed Minv of batches j mod 3 (pinned host
+    // memory), the event marking each one's launch complete, and the host
+    // threads that expand it to dense
+    float *minv_stage[3] = {};
+    size_t minv_stage_floats = 0;
+    cudaEvent_t batch_done[3] = {};
+    MinvExpander *expander = nullptr;
     DeviceBatch scratch;                // frg_gradient_batched descriptors
     double *f64_buf = nullptr;          // frg_verify_f64 scratch (frg::kSlotN doubles per knot)
     size_t f64_buf_doubles = 0;

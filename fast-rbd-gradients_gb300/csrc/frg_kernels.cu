@@ -23,11 +23,15 @@ struct PlainArgs {
     float *dqdd_relay = nullptr;  // RELAY: final dqdd destination (host memory)
 };
 
+template <bool MINV_PACKED = false>
 __device__ __forceinline__ KnotPtrs plain_knot(const PlainArgs &a, int tile, int lane) {
     const long long g = static_cast<long long>(tile) * 32 + lane;
     if (g >= a.n) return KnotPtrs{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    return KnotPtrs{a.q + kN * g, a.qd + kN * g, a.u + kN * g, a.dqdd + kDqddN * g, a.qdd + kN * g, a.minv + kMinvN * g};
+    constexpr int minv_stride = MINV_PACKED ? kMinvPackedN : kMinvN;
+    return KnotPtrs{a.q + kN * g,       a.qd + kN * g,  a.u + kN * g,
+                    a.dqdd + kDqddN * g, a.qdd + kN * g, a.minv + minv_stride * g};
 }
+static_assert(kMinvPackedN == kMinvPackedFloats, "host and kernel agree on the packed Minv width");
 
 // Floats of `p` that precede it in its 128-byte line.  A warp loop over
 // e = lane - line_shift(p) + 32 m stores exactly one whole line per step,
@@ -60,7 +64,9 @@ __device__ __forceinline__ void relay_dqdd(const PlainArgs &a, int tile, int lan
     __syncwarp();
 }
 
-template <bool DAMP, bool MPC, bool RELAY = false>
+// MINV_PACKED (host-buffer batches only): a.minv receives Minv's packed
+// upper triangle, kMinvPackedN floats per knot.
+template <bool DAMP, bool MPC, bool RELAY = false, bool MINV_PACKED = false>
 __global__ void __launch_bounds__(kMaxWarpsPerCta * 32) grad_plain_kernel(PlainArgs a) {
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -68,8 +74,8 @@ __global__ void __launch_bounds__(kMaxWarpsPerCta * 32) grad_plain_kernel(PlainA
     const int warps_per_cta = blockDim.x >> 5;
     const int ntiles = (a.n + 31) / 32;
     for (int tile = blockIdx.x * warps_per_cta + warp; tile < ntiles; tile += gridDim.x * warps_per_cta) {
-        const KnotPtrs kp = plain_knot(a, tile, lane);
-        process_tile<DAMP, MPC>(ws, lane, kp);
+        const KnotPtrs kp = plain_knot<MINV_PACKED>(a, tile, lane);
+        process_tile<DAMP, MPC, false, false, false, MINV_PACKED>(ws, lane, kp);
         // scatter_out ended with __syncwarp: every lane's dqdd stores are visible to the warp
         if constexpr (RELAY) relay_dqdd(a, tile, lane);
     }
@@ -127,12 +133,12 @@ cudaError_t prepare(K kernel) {
                                 cudaSharedmemCarveoutMaxShared);
 }
 
-template <bool D, bool M, bool R = false>
+template <bool D, bool M, bool R = false, bool P = false>
 cudaError_t plain_impl(const LaunchShape &sh, const PlainArgs &a, cudaStream_t st) {
     const int warps = sh.warps_per_cta;
     const int ntiles = (a.n + 31) / 32;
     const int grid = (ntiles + warps - 1) / warps;
-    grad_plain_kernel<D, M, R><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(a);
+    grad_plain_kernel<D, M, R, P><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -159,6 +165,10 @@ cudaError_t init_kernels() {
                           prepare(grad_plain_kernel<false, true>), prepare(grad_plain_kernel<true, true>),
                           prepare(grad_plain_kernel<false, false, true>), prepare(grad_plain_kernel<true, false, true>),
                           prepare(grad_plain_kernel<false, true, true>), prepare(grad_plain_kernel<true, true, true>),
+                          prepare(grad_plain_kernel<false, false, true, true>),
+                          prepare(grad_plain_kernel<true, false, true, true>),
+                          prepare(grad_plain_kernel<false, true, true, true>),
+                          prepare(grad_plain_kernel<true, true, true, true>),
                           prepare(grad_ragged_kernel<false, false>), prepare(grad_ragged_kernel<true, false>),
                           prepare(grad_ragged_kernel<false, true>), prepare(grad_ragged_kernel<true, true>)})
         if (r != cudaSuccess && e == cudaSuccess) e = r;
@@ -191,13 +201,21 @@ cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n
 
 cudaError_t launch_host_out(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
                             const float *u, float *dqdd_dev, float *dqdd, float *qdd, float *minv,
-                            cudaStream_t stream) {
+                            cudaStream_t stream, bool minv_packed) {
     if (n <= 0) return cudaSuccess;
     if (shape.warps_per_cta < 1 || shape.warps_per_cta > kMaxWarpsPerCta) return cudaErrorInvalidValue;
-    if (shape.lanes_per_knot == 8)  // small batches: latency first, every result straight to its destination
+    if (shape.lanes_per_knot == 8) {  // small batches: latency first, every result straight to its destination
+        if (minv_packed) return cudaErrorInvalidValue;
         return launch_group_plain(damping, mpc, shape, n, q, qd, u, dqdd, qdd, minv, stream);
+    }
     PlainArgs a{q, qd, u, dqdd_dev, qdd, minv, n};
     a.dqdd_relay = dqdd;
+    if (minv_packed) {
+        if (!damping && !mpc) return plain_impl<false, false, true, true>(shape, a, stream);
+        if (damping && !mpc) return plain_impl<true, false, true, true>(shape, a, stream);
+        if (!damping && mpc) return plain_impl<false, true, true, true>(shape, a, stream);
+        return plain_impl<true, true, true, true>(shape, a, stream);
+    }
     if (!damping && !mpc) return plain_impl<false, false, true>(shape, a, stream);
     if (damping && !mpc) return plain_impl<true, false, true>(shape, a, stream);
     if (!damping && mpc) return plain_impl<false, true, true>(shape, a, stream);

@@ -56,9 +56,11 @@ cudaError_t launch_plain(bool damping, bool mpc, const LaunchShape &shape, int n
 // minv are read and written in place across the host link; dqdd is computed
 // into dqdd_dev (device, [n][2N^2]) and each finished tile is copied to dqdd as
 // whole lines.  The latency mapping writes every result in place directly.
+// minv_packed (throughput mapping only): minv receives Minv's upper triangle,
+// kMinvPackedN floats per knot.
 cudaError_t launch_host_out(bool damping, bool mpc, const LaunchShape &shape, int n, const float *q, const float *qd,
                             const float *u, float *dqdd_dev, float *dqdd, float *qdd, float *minv,
-                            cudaStream_t stream);
+                            cudaStream_t stream, bool minv_packed = false);
 
 // Ragged batch: one persistent launch walking 32-knot tiles of the
 // concatenated knot list.  segs[nseg + 1] (last = end sentinel with

@@ -27,6 +27,7 @@ constexpr int kLinkSlots = kSlotsPerLink * kJoints;
 // 3N inputs, or its 6N external-force values
 constexpr int kStageFloats = kJoints * kJoints > 6 * kJoints ? kJoints * kJoints : 6 * kJoints;
 constexpr int kMinvFloats = kJoints * kJoints;
+constexpr int kMinvPackedFloats = kJoints * ((kJoints + 2) / 2);  // upper triangle, padded to groups of N
 constexpr int kDqddFloats = 2 * kJoints * kJoints;
 
 // Four reals as one 16-byte-aligned shared-memory slot.
@@ -773,8 +774,11 @@ __device__ __forceinline__ void minv_times(real out[kJoints], const real Mi[kJoi
 // from a trajectory's device slot into it, and sends results to the pinned
 // host slot when the caller asked for them); a mirror that no lane of the
 // tile wants is skipped.  With FEXT, kp.fext holds each knot's external link
-// forces; with FDONLY only q̈ and Minv are produced (forward dynamics).
-template <bool DAMP, bool MPC, bool MIRROR = false, bool FEXT = false, bool FDONLY = false>
+// forces; with FDONLY only q̈ and Minv are produced (forward dynamics); with
+// MINV_PACKED, kp.minv receives Minv's upper triangle (kMinvPackedFloats per
+// knot, column by column) instead of the dense matrix.
+template <bool DAMP, bool MPC, bool MIRROR = false, bool FEXT = false, bool FDONLY = false,
+          bool MINV_PACKED = false>
 __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotPtrs &kp,
                                              const KnotPtrs &mr = KnotPtrs{}) {
     constexpr int N = kJoints, NN = kMinvFloats;
@@ -814,13 +818,26 @@ __device__ __forceinline__ void process_tile(WarpSmem *ws, int lane, const KnotP
     if constexpr (FEXT && !FDONLY) rnea_with_qdd<MPC, FEXT>(ws, lane, qd, qdd, sq, cq, fx);
     __syncwarp();
 
-    // Minv (dense) and qdd out
+    // Minv (dense, or its packed upper triangle) and qdd out
+    if constexpr (MINV_PACKED) {
+        static_assert(!MIRROR, "the server's slots hold dense Minv");
+        constexpr int P = kMinvPackedFloats;
+        static_assert(P <= kStageFloats && P % N == 0, "packed Minv rows fit the staging buffer in groups of N");
 #pragma unroll
-    for (int c = 0; c < N; c++)
+        for (int c = 0, e = 0; c < N; c++)
 #pragma unroll
-        for (int r = 0; r < N; r++) ws->stage[lane * NN + r + N * c] = r <= c ? Mi[r][c] : Mi[c][r];
-    scatter_out<NN>(ws->stage, kp.minv, lane, ws->knot);
-    if (MIRROR && mirror_out) scatter_out<NN>(ws->stage, mr.minv, lane, ws->knot);
+            for (int r = 0; r <= c; r++, e++) ws->stage[lane * P + e] = Mi[r][c];
+#pragma unroll
+        for (int e = N * (N + 1) / 2; e < P; e++) ws->stage[lane * P + e] = real(0);
+        scatter_out<P>(ws->stage, kp.minv, lane, ws->knot);
+    } else {
+#pragma unroll
+        for (int c = 0; c < N; c++)
+#pragma unroll
+            for (int r = 0; r < N; r++) ws->stage[lane * NN + r + N * c] = r <= c ? Mi[r][c] : Mi[c][r];
+        scatter_out<NN>(ws->stage, kp.minv, lane, ws->knot);
+        if (MIRROR && mirror_out) scatter_out<NN>(ws->stage, mr.minv, lane, ws->knot);
+    }
 #pragma unroll
     for (int r = 0; r < N; r++) ws->stage[lane * N + r] = qdd[r];
     scatter_out<N>(ws->stage, kp.qdd, lane, ws->knot);

@@ -160,11 +160,16 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
  * between two internal streams, two launches in flight at once, so a batch's
  * launch and first tiles -- about 25 us in which no result exists yet -- overlap
  * the previous batch's results streaming over the host link, which then stays
- * busy.  Batches must not share output arrays with other batches of the call
- * that may be in flight (neighbouring ones).  A batch's qdd and minv may be
- * NULL, as in frg_gradient_host.  Pageable arrays are processed one
- * batch after the other.  No counterpart in the reference, whose
- * time_GPU.cu:310-330 loop synchronises after every batch.
+ * busy.  When every batch asks for Minv (and the context runs one lane per
+ * knot), Minv crosses the link as its upper triangle -- 112 instead of 196 B
+ * per knot at 7 joints -- into pinned staging owned by ctx, and host threads
+ * expand each batch into its dense minv array while later batches compute:
+ * the same bits, 14 % fewer bytes on the link that bounds the call.  Batches
+ * must not share output arrays with other batches of the call that may be in
+ * flight (neighbouring ones).  A batch's qdd and minv may be NULL, as in
+ * frg_gradient_host.  Pageable arrays are processed one batch after the
+ * other.  No counterpart in the reference, whose time_GPU.cu:310-330 loop
+ * synchronises after every batch.
  */
 typedef struct frg_host_batch {
     int n_knots;

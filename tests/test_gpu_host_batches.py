@@ -114,3 +114,48 @@ def test_results_not_asked_for_are_not_returned(pinned, lanes):
     finally:
         for p in owned:
             native.lib().frg_host_free(p)
+
+
+@pytest.mark.parametrize("lanes", [1, 8])
+def test_packed_minv_batches_match_single_calls_bitwise(lanes):
+    """Every batch returns Minv: with one lane per knot the call sends Minv's
+    upper triangle and expands it on the host (some batches without q̈, so
+    q̈ also goes to the relay's tail); the dense results carry the single
+    call's bits, Minv exactly symmetric."""
+    sizes = [3000, 64, 1, 4097, 777]
+    data = [frg.sample_knots(n, seed=120 + i) for i, n in enumerate(sizes)]
+    owned = []
+    try:
+        with frg.Context() as ctx:
+            ctx.set_lanes_per_knot(lanes)
+            want = [ctx.gradient_host(q, qd, u) for q, qd, u in data]
+            batches, outs = [], []
+            for i, ((q, qd, u), n) in enumerate(zip(data, sizes)):
+                ins = []
+                for x in (q, qd, u):
+                    p, a = _pinned(x.shape)
+                    owned.append(p)
+                    a[:] = x
+                    ins.append(a)
+                o = []
+                for w, keep in ((98, True), (7, i % 2 == 0), (49, True)):
+                    if keep:
+                        p, a = _pinned((n, w))
+                        owned.append(p)
+                        a[:] = np.nan
+                        o.append(a)
+                    else:
+                        o.append(None)
+                batches.append((n, *ins, *o))
+                outs.append(o)
+            for _ in range(2):  # the second call reuses the staging buffers and expansion threads
+                ctx.gradient_host_batches(batches)
+                for o, w in zip(outs, want):
+                    for a, b in zip(o, w):
+                        if a is not None:
+                            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+                    m = o[2].reshape(-1, 7, 7)
+                    assert np.array_equal(m, m.transpose(0, 2, 1))
+    finally:
+        for p in owned:
+            native.lib().frg_host_free(p)
