@@ -540,7 +540,7 @@ def run_frg(args):
         for ptr, arr in zip(hin, (q, qd, u)):
             np.ctypeslib.as_array((ctypes.c_float * (7 * n)).from_address(ptr))[:] = arr.reshape(-1)
         hsets.append(hin + hout)
-    e2e_steps = max(5, args.steps // 5)
+    e2e_steps = max(5, args.steps)  # K steps, each the whole mix from host buffers to host buffers
     # one frg_gradient_host call per step (synchronous: launch, results, return)
     for _ in range(max(1, args.warmup)):
         ctx.gradient_host_into(n, *hsets[0])

@@ -159,3 +159,42 @@ def test_packed_minv_batches_match_single_calls_bitwise(lanes):
     finally:
         for p in owned:
             native.lib().frg_host_free(p)
+
+
+@pytest.mark.parametrize("want_qdd", [True, False])
+def test_large_single_call_runs_chunked_with_the_same_bits(want_qdd):
+    """A single frg_gradient_host of 70,000 knots on pinned arrays runs as
+    pipelined chunks (packed Minv expanded on the host); its results equal a
+    device-array launch bitwise."""
+    import torch
+    n = 70000
+    q, qd, u = frg.sample_knots(n, seed=321)
+    owned = []
+    try:
+        ins = []
+        for x in (q, qd, u):
+            p, a = _pinned(x.shape)
+            owned.append(p)
+            a[:] = x
+            ins.append(a)
+        outs = []
+        for w, keep in ((98, True), (7, want_qdd), (49, True)):
+            if keep:
+                p, a = _pinned((n, w))
+                owned.append(p)
+                a[:] = np.nan
+                outs.append(a)
+            else:
+                outs.append(None)
+        with frg.Context() as ctx:
+            ctx.gradient_host_into(n, *ins, *outs)
+            tq, tqd, tu = (torch.from_numpy(x).cuda() for x in (q, qd, u))
+            dev = [torch.empty((n, w), device="cuda") for w in (98, 7, 49)]
+            ctx.gradient(n, tq, tqd, tu, *dev)
+            torch.cuda.synchronize()
+        for a, b in zip(outs, dev):
+            if a is not None:
+                assert np.array_equal(a.view(np.uint32), b.cpu().numpy().view(np.uint32))
+    finally:
+        for p in owned:
+            native.lib().frg_host_free(p)
