@@ -516,10 +516,6 @@ HostOuts host_outs(float *relay, size_t n, float *qdd, float *minv) {
 
 bool host_or_null_accessible(const void *p) { return !p || device_accessible(p); }
 
-// frg_gradient_host on pinned arrays of at least this many knots runs as up to
-// 8 pipelined chunks of at least a quarter of it.
-constexpr size_t kChunkedHostKnots = 32768;
-
 }  // namespace
 
 frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const float *qd, const float *u,
@@ -541,23 +537,6 @@ frg_status frg_gradient_host(frg_ctx *ctx, int n_knots, const float *q, const fl
     // device-to-host rate (about 190 GB/s here) bounds the call.
     if (device_accessible(q) && device_accessible(qd) && device_accessible(u) && device_accessible(dqdd) &&
         host_or_null_accessible(qdd) && host_or_null_accessible(minv)) {
-        // A large call with Minv runs as pipelined chunks of whole tiles
-        // (frg_gradient_host_batches: Minv over the link packed, expanded on
-        // host threads while later chunks stream; one launch's start and the
-        // last chunk's expansion stay exposed).
-        if (minv && ctx->shape.lanes_per_knot == 1 && n >= kChunkedHostKnots) {
-            const int chunks = static_cast<int>(std::min<size_t>(8, n / (kChunkedHostKnots / 4)));
-            const size_t per = (n / chunks + 31) / 32 * 32;
-            frg_host_batch list[8];
-            int m = 0;
-            for (size_t k0 = 0; k0 < n; k0 += per, m++) {
-                const size_t c = std::min(per, n - k0);
-                list[m] = frg_host_batch{static_cast<int>(c), q + frg::kN * k0, qd + frg::kN * k0, u + frg::kN * k0,
-                                         dqdd + frg::kDqddN * k0, qdd ? qdd + frg::kN * k0 : nullptr,
-                                         minv + frg::kMinvN * k0};
-            }
-            return frg_gradient_host_batches(ctx, m, list);
-        }
         if (!ensure_floats(ctx, &ctx->host_buf, &ctx->host_buf_floats, relay_floats(n, qdd, minv),
                            "frg_gradient_host"))
             return FRG_ERR_OUT_OF_MEMORY;

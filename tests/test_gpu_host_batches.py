@@ -162,10 +162,10 @@ def test_packed_minv_batches_match_single_calls_bitwise(lanes):
 
 
 @pytest.mark.parametrize("want_qdd", [True, False])
-def test_large_single_call_runs_chunked_with_the_same_bits(want_qdd):
-    """A single frg_gradient_host of 70,000 knots on pinned arrays runs as
-    pipelined chunks (packed Minv expanded on the host); its results equal a
-    device-array launch bitwise."""
+def test_large_single_call_matches_device_launch_bitwise(want_qdd):
+    """A single frg_gradient_host of 70,000 knots on pinned arrays (results
+    streamed from the kernel as tiles finish) equals a device-array launch
+    bitwise."""
     import torch
     n = 70000
     q, qd, u = frg.sample_knots(n, seed=321)
