@@ -6,7 +6,7 @@ u ~ U(-20, 20) (seeded synthetic data; the reference ships no dataset) --
 through the full path (RNEA, Minv, q̈, dtau/dq, dtau/dqd, -Minv dtau) in FP32.
 
   value     knot-gradients/s of the batched form: one persistent launch over
-            the ragged offset list, replayed as a CUDA graph, inputs resident
+            the ragged offset list (a plan launch per step), inputs resident
             in HBM; 6 rotating input/output sets (~280 MB > 129 MB L2).
   e2e       the same metric through the C ABI's host-buffer calls: H2D of
             q, qd, u from pinned memory, kernel, D2H of dqdd, qdd, Minv
@@ -480,7 +480,7 @@ def run_frg(args):
         """CUDA-event time (ms) on `stream` of `steps` calls issued back to
         back between one pair of events, as a list of `steps` equal per-step
         shares.  (Bracketing every step with its own events instead adds the
-        stream's event processing, about 4 us, to each graph replay.)"""
+        stream's event processing, about 4 us, to each launch.)"""
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for i in range(steps):
@@ -598,7 +598,7 @@ def run_frg(args):
             "config": {
                 "workload": f"ragged mix: {n_traj} trajectories, horizons U{{{H_LO}..{H_HI}}} (seed {MIX_SEED}), "
                             f"{n} knots per rank, stored in shuffled order; one persistent launch over the "
-                            f"ragged trajectory list, replayed as a CUDA graph",
+                            f"ragged trajectory list, one plan launch per step",
                 "knots_per_step": n, "l2": f"{ROTATING_SETS} rotating input/output sets "
                                             f"({ROTATING_SETS * n * BYTES_PER_KNOT / 1e6:.0f} MB > 129 MB L2)",
                 "launch_shape": tuning,

@@ -1,5 +1,5 @@
 // C ABI of the engine (include/frg.h): contexts, the plain / host / batched
-// calls, plans captured as CUDA graphs, and the launch-shape autotuner.
+// calls, plans, and the launch-shape autotuner.
 #include "frg.h"
 
 #include <cuda_runtime.h>

@@ -4,6 +4,7 @@
 // spread over 8x more warps.
 #include "frg_kernels.cuh"
 #include "frg_knot_group.cuh"
+#include "frg_launch.cuh"
 #include "frg_serve.cuh"
 
 namespace frg {
@@ -26,6 +27,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32)
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     GroupSmem *gs = reinterpret_cast<GroupSmem *>(smem_raw) + warp;
+    dependent_launch_begin();
     const long long items = (static_cast<long long>(n) + kGroupKnots - 1) / kGroupKnots;
     const int wpc = blockDim.x >> 5;
     for (long long it = static_cast<long long>(blockIdx.x) * wpc + warp; it < items;
@@ -57,6 +59,7 @@ __device__ __forceinline__ void group_persistent(const Seg *segs, int nseg, cons
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     GroupSmem *gs = reinterpret_cast<GroupSmem *>(smem_raw) + warp;
+    dependent_launch_begin();
     const unsigned int items = static_cast<unsigned int>(ntiles) * 8u;
     for (unsigned int ticket; next_ticket(items, counter, lane, ticket);) {
         const int tile = static_cast<int>(ticket >> 3), slice = static_cast<int>(ticket & 7u);
@@ -141,10 +144,10 @@ cudaError_t launch_group_plain(bool damping, bool mpc, const LaunchShape &sh, in
     const long long items = (static_cast<long long>(n) + kGroupKnots - 1) / kGroupKnots;
     const int grid = static_cast<int>((items + w - 1) / w);
     const size_t smem = sizeof(GroupSmem) * w;
-#define FRG_CALL(D, M) grad_group_plain_kernel<D, M><<<grid, w * 32, smem, st>>>(q, qd, u, dqdd, qdd, minv, n);
+#define FRG_CALL(D, M) \
+    return launch_dependent(grad_group_plain_kernel<D, M>, dim3(grid), dim3(w * 32), smem, st, q, qd, u, dqdd, qdd, minv, n);
     FRG_DISPATCH(damping, mpc, FRG_CALL)
 #undef FRG_CALL
-    return cudaGetLastError();
 }
 
 cudaError_t launch_group_single_knot(bool damping, bool mpc, int iters, const float *q, const float *qd,
@@ -162,10 +165,11 @@ cudaError_t launch_group_ragged(bool damping, bool mpc, const LaunchShape &sh, i
     if (ntiles <= 0) return cudaSuccess;
     const int w = sh.warps_per_cta, grid = persistent_grid(sh, num_sms, static_cast<long long>(ntiles) * 8);
     const size_t smem = sizeof(GroupSmem) * w;
-#define FRG_CALL(D, M) grad_group_ragged_kernel<D, M><<<grid, w * 32, smem, st>>>(segs, nseg, tile_seg, ntiles, counter);
+#define FRG_CALL(D, M) \
+    return launch_dependent(grad_group_ragged_kernel<D, M>, dim3(grid), dim3(w * 32), smem, st, segs, nseg, tile_seg, \
+                            ntiles, counter);
     FRG_DISPATCH(damping, mpc, FRG_CALL)
 #undef FRG_CALL
-    return cudaGetLastError();
 }
 
 cudaError_t launch_group_serve(bool damping, bool mpc, const LaunchShape &sh, int num_sms, const ServeSegment *segs,
@@ -173,10 +177,11 @@ cudaError_t launch_group_serve(bool damping, bool mpc, const LaunchShape &sh, in
     if (ntiles <= 0) return cudaSuccess;
     const int w = sh.warps_per_cta, grid = persistent_grid(sh, num_sms, static_cast<long long>(ntiles) * 8);
     const size_t smem = sizeof(GroupSmem) * w;
-#define FRG_CALL(D, M) grad_group_serve_kernel<D, M><<<grid, w * 32, smem, st>>>(segs, nseg, tile_seg, ntiles, counter);
+#define FRG_CALL(D, M) \
+    return launch_dependent(grad_group_serve_kernel<D, M>, dim3(grid), dim3(w * 32), smem, st, segs, nseg, tile_seg, \
+                            ntiles, counter);
     FRG_DISPATCH(damping, mpc, FRG_CALL)
 #undef FRG_CALL
-    return cudaGetLastError();
 }
 
 }  // namespace frg

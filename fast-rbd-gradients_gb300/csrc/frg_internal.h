@@ -78,7 +78,7 @@ struct frg_plan {
     long long nknots = 0;
     bool contiguous = false;
     frg_traj whole{};
-    cudaGraphExec_t exec = nullptr;
+    frg::LaunchShape shape;  // the context's shape when the plan was made
 };
 
 void frg_set_error(frg_ctx *ctx, const std::string &msg);

@@ -6,6 +6,7 @@
 // q̈ and Minv computed on the device, and no block barrier at all.
 #include "frg_kernels.cuh"
 #include "frg_knot.cuh"
+#include "frg_launch.cuh"
 
 namespace frg {
 
@@ -71,6 +72,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerCta * 32) grad_plain_kernel(PlainA
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    dependent_launch_begin();
     const int warps_per_cta = blockDim.x >> 5;
     const int ntiles = (a.n + 31) / 32;
     for (int tile = blockIdx.x * warps_per_cta + warp; tile < ntiles; tile += gridDim.x * warps_per_cta) {
@@ -98,6 +100,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerCta * 32)
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    dependent_launch_begin();  // before the first ticket: the previous launch of this list resets the counter
     for (unsigned int tile; next_ticket(static_cast<unsigned int>(ntiles), counter, lane, tile);)
         process_tile<DAMP, MPC>(ws, lane, ragged_knot(segs, nseg, tile_seg, static_cast<int>(tile), lane));
 }
@@ -138,8 +141,8 @@ cudaError_t plain_impl(const LaunchShape &sh, const PlainArgs &a, cudaStream_t s
     const int warps = sh.warps_per_cta;
     const int ntiles = (a.n + 31) / 32;
     const int grid = (ntiles + warps - 1) / warps;
-    grad_plain_kernel<D, M, R, P><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(a);
-    return cudaGetLastError();
+    return launch_dependent(grad_plain_kernel<D, M, R, P>, dim3(grid), dim3(warps * 32), sizeof(WarpSmem) * warps, st,
+                            a);
 }
 
 template <bool D, bool M>
@@ -150,9 +153,8 @@ cudaError_t ragged_impl(const LaunchShape &sh, int num_sms, const Segment *segs,
     const int needed = (ntiles + warps - 1) / warps;
     if (grid > needed) grid = needed;
     if (grid < 1) grid = 1;
-    grad_ragged_kernel<D, M><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(segs, nseg, tile_seg, ntiles,
-                                                                                  counter);
-    return cudaGetLastError();
+    return launch_dependent(grad_ragged_kernel<D, M>, dim3(grid), dim3(warps * 32), sizeof(WarpSmem) * warps, st, segs,
+                            nseg, tile_seg, ntiles, counter);
 }
 
 }  // namespace

@@ -68,7 +68,7 @@ struct KnotPtrs {
 //     for (unsigned int t; next_ticket(items, counter, lane, t);) work(t);
 // until the `items` work items are exhausted.  The warp that draws the very
 // last ticket (items + total warps - 1: every warp draws one failing ticket)
-// resets the counter, so back-to-back and graph-replayed launches need no
+// resets the counter, so back-to-back and repeated plan launches need no
 // memset.
 __device__ __forceinline__ bool next_ticket(unsigned int items, unsigned int *counter, int lane,
                                             unsigned int &ticket) {

@@ -1,5 +1,5 @@
-// Plans (batched launches prepared once and replayed as CUDA graphs) and the
-// launch-shape autotuner.
+// Plans (batched launches prepared once: descriptor lists on the device, launch
+// shape fixed) and the launch-shape autotuner.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,23 +21,19 @@ bool ok(frg_ctx *ctx, cudaError_t e, const char *what) {
     return false;
 }
 
-// Captures one batched launch of `plan` into an executable graph.
-bool capture(frg_plan *plan) {
+// One launch of a plan, with the launch shape the context had when the plan
+// was made.  A direct launch rather than a graph replay: launched with
+// programmatic stream serialization (frg_launch.cuh), a plan launch that
+// follows another on the stream starts while the earlier one's last tiles
+// finish, which a graph launch cannot do (6 % of a launch over the 512-mix).
+cudaError_t plan_launch(frg_plan *plan, cudaStream_t st) {
     frg_ctx *ctx = plan->ctx;
-    cudaStream_t cs = nullptr;
-    if (!ok(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream")) return false;
-    bool good = ok(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-    cudaGraph_t graph = nullptr;
-    if (good) {
-        cudaError_t le = plan->contiguous ? frg_launch_whole(ctx, plan->whole, cs)
-                                          : frg_launch_batch(ctx, plan->dev, plan->nseg, plan->ntiles, cs);
-        cudaError_t ee = cudaStreamEndCapture(cs, &graph);
-        good = ok(ctx, le, "batched launch capture") && ok(ctx, ee, "cudaStreamEndCapture");
-    }
-    if (good) good = ok(ctx, cudaGraphInstantiate(&plan->exec, graph, 0), "cudaGraphInstantiate");
-    if (graph) cudaGraphDestroy(graph);
-    cudaStreamDestroy(cs);
-    return good;
+    if (plan->contiguous)
+        return frg::launch_plain(ctx->damping, ctx->mpc, plan->shape, static_cast<int>(plan->whole.n_knots),
+                                 plan->whole.q, plan->whole.qd, plan->whole.u, plan->whole.dqdd, plan->whole.qdd,
+                                 plan->whole.minv, st);
+    return frg::launch_ragged(ctx->damping, ctx->mpc, plan->shape, ctx->num_sms, plan->dev.segs, plan->nseg,
+                              plan->dev.tile_seg, plan->ntiles, plan->dev.counter, st);
 }
 
 }  // namespace
@@ -70,11 +66,8 @@ frg_status frg_plan_create(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_
         return FRG_OK;
     }
     DeviceGuard g(ctx->device);
+    plan->shape = plan->contiguous ? ctx->shape : ctx->ragged_shape;
     if (plan->contiguous) {  // one plain launch: no descriptor lists on the device
-        if (!capture(plan)) {
-            frg_plan_destroy(plan);
-            return FRG_ERR_CUDA;
-        }
         *out = plan;
         return FRG_OK;
     }
@@ -87,8 +80,7 @@ frg_status frg_plan_create(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_
     if (!ok(ctx, cudaMemcpy(plan->dev.segs, hb.segs.data(), sizeof(frg::Segment) * hb.segs.size(), cudaMemcpyHostToDevice),
             "plan segment upload") ||
         !ok(ctx, cudaMemcpy(plan->dev.tile_seg, hb.tile_seg.data(), sizeof(int) * hb.tile_seg.size(), cudaMemcpyHostToDevice),
-            "plan tile upload") ||
-        !capture(plan)) {
+            "plan tile upload")) {
         frg_plan_destroy(plan);
         return FRG_ERR_CUDA;
     }
@@ -111,7 +103,7 @@ frg_status frg_plan_launch(frg_plan *plan, frg_stream stream) {
     if (!plan) return FRG_ERR_INVALID_ARGUMENT;
     if (plan->nknots == 0) return FRG_OK;
     DeviceGuard g(plan->ctx->device);
-    if (!ok(plan->ctx, cudaGraphLaunch(plan->exec, stream), "cudaGraphLaunch")) return FRG_ERR_CUDA;
+    if (!ok(plan->ctx, plan_launch(plan, reinterpret_cast<cudaStream_t>(stream)), "frg_plan_launch")) return FRG_ERR_CUDA;
     return FRG_OK;
 }
 
@@ -121,7 +113,6 @@ void frg_plan_destroy(frg_plan *plan) {
     if (!plan) return;
     {
         DeviceGuard g(plan->ctx->device);
-        if (plan->exec) cudaGraphExecDestroy(plan->exec);
         plan->dev.release();
     }
     delete plan;

@@ -5,6 +5,7 @@
 // asked for, to the host slot, so a batch needs no per-call copy.
 #include "frg_kernels.cuh"
 #include "frg_knot.cuh"
+#include "frg_launch.cuh"
 #include "frg_serve.cuh"
 
 namespace frg {
@@ -17,6 +18,7 @@ __global__ void __launch_bounds__(8 * 32)
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    dependent_launch_begin();
     for (unsigned int tile; next_ticket(static_cast<unsigned int>(ntiles), counter, lane, tile);) {
         const long long g = static_cast<long long>(tile) * 32 + lane;
         KnotPtrs kp{}, mr{};
@@ -45,8 +47,8 @@ cudaError_t serve_impl(const LaunchShape &sh, int num_sms, const ServeSegment *s
     const int needed = (ntiles + warps - 1) / warps;
     if (grid > needed) grid = needed;
     if (grid < 1) grid = 1;
-    grad_serve_kernel<D, M><<<grid, warps * 32, sizeof(WarpSmem) * warps, st>>>(segs, nseg, tile_seg, ntiles, counter);
-    return cudaGetLastError();
+    return launch_dependent(grad_serve_kernel<D, M>, dim3(grid), dim3(warps * 32), sizeof(WarpSmem) * warps, st, segs,
+                            nseg, tile_seg, ntiles, counter);
 }
 
 }  // namespace

@@ -285,10 +285,16 @@ frg_status frg_gradient_ragged_noalloc(frg_ctx *ctx, int n_traj, const int64_t *
                                        frg_stream stream);
 
 /*
- * Plans: a batched launch prepared once (descriptor list on the device, CUDA
- * graph captured on first launch) and replayed by frg_plan_launch.  The
- * trajectory pointers are baked in; the data behind them may change between
- * launches.  Launches of one plan must not overlap on the device.
+ * Plans: a batched launch prepared once (descriptor list on the device, the
+ * context's launch shape at creation) and repeated by frg_plan_launch, one
+ * persistent launch each.  The trajectory pointers are baked in; the data
+ * behind them may change between launches.  Launches of one plan must not
+ * overlap on the device.  Every launch of the engine's gradient kernels uses
+ * programmatic dependent launch: it may be scheduled while the previous work
+ * on its stream finishes, and waits for that work to complete before reading
+ * or writing anything, so stream order holds and back-to-back launches (solver
+ * iterations, plan repeats) lose no time between them.  Plan launches can be
+ * captured into a caller's CUDA graph like any kernel launch.
  */
 frg_status frg_plan_create(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_plan **out);
 frg_status frg_plan_create_ragged(frg_ctx *ctx, int n_traj, const int64_t *offsets, const float *q,
