@@ -13,6 +13,7 @@
 // N = kN joints (frg_dims.h).
 #include "frg_kernels.cuh"
 #include "frg_knot.cuh"
+#include "frg_launch.cuh"
 
 namespace frg {
 
@@ -25,6 +26,7 @@ __global__ void __launch_bounds__(8 * 32)
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    dependent_launch_begin();
     const int wpc = blockDim.x >> 5, ntiles = (n + 31) / 32;
     for (int tile = blockIdx.x * wpc + warp; tile < ntiles; tile += gridDim.x * wpc) {
         const long long g = static_cast<long long>(tile) * 32 + lane;
@@ -47,6 +49,7 @@ __global__ void __launch_bounds__(8 * 32) grad_knots_kernel(float *knots, float 
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    dependent_launch_begin();
     const int wpc = blockDim.x >> 5, ntiles = (n + 31) / 32;
     for (int tile = blockIdx.x * wpc + warp; tile < ntiles; tile += gridDim.x * wpc) {
         const long long g = static_cast<long long>(tile) * 32 + lane;
@@ -170,8 +173,8 @@ template <bool D, bool M, bool F, bool O>
 cudaError_t launch_one(const LaunchShape &sh, int n, const float *q, const float *qd, const float *u,
                        const float *fext, float *dqdd, float *qdd, float *minv, cudaStream_t st) {
     const int w = sh.warps_per_cta, ntiles = (n + 31) / 32, grid = (ntiles + w - 1) / w;
-    grad_ext_kernel<D, M, F, O><<<grid, w * 32, sizeof(WarpSmem) * w, st>>>(q, qd, u, fext, dqdd, qdd, minv, n);
-    return cudaGetLastError();
+    return launch_dependent(grad_ext_kernel<D, M, F, O>, dim3(grid), dim3(w * 32), sizeof(WarpSmem) * w, st, q, qd, u,
+                            fext, dqdd, qdd, minv, n);
 }
 
 template <bool F, bool O>
@@ -243,11 +246,11 @@ cudaError_t launch_knots(bool damping, bool mpc, const LaunchShape &shape, int n
     if (shape.warps_per_cta < 1 || shape.warps_per_cta > 8) return cudaErrorInvalidValue;
     const int w = shape.warps_per_cta, ntiles = (n + 31) / 32, grid = (ntiles + w - 1) / w;
     const size_t smem = sizeof(WarpSmem) * w;
-    if (!damping && !mpc) grad_knots_kernel<false, false><<<grid, w * 32, smem, stream>>>(knots, dqdd, n);
-    else if (damping && !mpc) grad_knots_kernel<true, false><<<grid, w * 32, smem, stream>>>(knots, dqdd, n);
-    else if (!damping && mpc) grad_knots_kernel<false, true><<<grid, w * 32, smem, stream>>>(knots, dqdd, n);
-    else grad_knots_kernel<true, true><<<grid, w * 32, smem, stream>>>(knots, dqdd, n);
-    return cudaGetLastError();
+    auto kernel = !damping && !mpc  ? grad_knots_kernel<false, false>
+                  : damping && !mpc ? grad_knots_kernel<true, false>
+                  : !damping && mpc ? grad_knots_kernel<false, true>
+                                    : grad_knots_kernel<true, true>;
+    return launch_dependent(kernel, dim3(grid), dim3(w * 32), smem, stream, knots, dqdd, n);
 }
 
 cudaError_t launch_knot_status(int num_sms, int n, const float *q, const float *qd, const float *u,
