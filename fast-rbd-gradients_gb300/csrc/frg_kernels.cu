@@ -65,6 +65,16 @@ __device__ __forceinline__ void relay_dqdd(const PlainArgs &a, int tile, int lan
     __syncwarp();
 }
 
+// A lane's knot inputs into L2 (before the wait on the work ahead; see
+// prefetch_l2).  Idle lanes (q == nullptr) issue nothing.
+__device__ __forceinline__ void prefetch_knot_inputs(const KnotPtrs &kp) {
+    if (kp.q) {
+        prefetch_l2(kp.q);
+        prefetch_l2(kp.qd);
+        prefetch_l2(kp.u);
+    }
+}
+
 // MINV_PACKED (host-buffer batches only): a.minv receives Minv's packed
 // upper triangle, kMinvPackedN floats per knot.
 template <bool DAMP, bool MPC, bool RELAY = false, bool MINV_PACKED = false>
@@ -72,9 +82,12 @@ __global__ void __launch_bounds__(kMaxWarpsPerCta * 32) grad_plain_kernel(PlainA
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
-    dependent_launch_begin();
     const int warps_per_cta = blockDim.x >> 5;
     const int ntiles = (a.n + 31) / 32;
+    // inputs in device memory: the first tile's into L2 while the work ahead finishes
+    if (!RELAY && blockIdx.x * warps_per_cta + warp < ntiles)
+        prefetch_knot_inputs(plain_knot<MINV_PACKED>(a, blockIdx.x * warps_per_cta + warp, lane));
+    dependent_launch_begin();
     for (int tile = blockIdx.x * warps_per_cta + warp; tile < ntiles; tile += gridDim.x * warps_per_cta) {
         const KnotPtrs kp = plain_knot<MINV_PACKED>(a, tile, lane);
         process_tile<DAMP, MPC, false, false, false, MINV_PACKED>(ws, lane, kp);
@@ -100,6 +113,12 @@ __global__ void __launch_bounds__(kMaxWarpsPerCta * 32)
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
+    // The tile this warp is likely to draw first (warps draw their first
+    // tickets in about this order) has its inputs brought into L2 while the
+    // work ahead finishes.  The descriptors it reads are written only by the
+    // host, by copies that the launch waits for in full.
+    const int first = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (first < ntiles) prefetch_knot_inputs(ragged_knot(segs, nseg, tile_seg, first, lane));
     dependent_launch_begin();  // before the first ticket: the previous launch of this list resets the counter
     for (unsigned int tile; next_ticket(static_cast<unsigned int>(ntiles), counter, lane, tile);)
         process_tile<DAMP, MPC>(ws, lane, ragged_knot(segs, nseg, tile_seg, static_cast<int>(tile), lane));

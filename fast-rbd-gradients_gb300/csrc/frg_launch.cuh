@@ -20,6 +20,15 @@ __device__ __forceinline__ void dependent_launch_begin() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
+// Brings the line holding p into L2.  Only a hint: a kernel may issue it
+// before dependent_launch_begin() for the inputs of its first tile, so their
+// DRAM latency overlaps the end of the work ahead of it on the stream.  The
+// loads that use the data come after the wait, and L2 is the GPU's point of
+// coherence, so an input that the work ahead still writes is read correctly.
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 template <typename... KArgs, typename... Args>
 cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
                              Args... args) {

@@ -263,6 +263,46 @@ def test_back_to_back_launches_keep_stream_order():
         assert torch.equal(a, b)
 
 
+def test_plans_prepared_ahead_chain_without_synchronisation():
+    """Plans prepared before the chain launch back to back, each reading the
+    previous plan's q̈ output as its joint angles: the persistent kernel brings
+    its first tile's inputs into L2 before it waits for the launch ahead of it,
+    and still reads the finished values.  Checked against the same chain with a
+    device synchronisation after every launch, also with plain launches
+    (which prefetch too) between the plans."""
+    import torch
+    h, off = frg.ragged_horizons(128, 8, 256, seed=60)
+    n = int(off[-1])
+    q, qd, u = frg.sample_knots(n, seed=61)
+    tqd, tu = (torch.from_numpy(x).cuda() for x in (qd, u))
+
+    def chain(sync, with_plain):
+        steps = 6
+        bufs = [torch.from_numpy(q).cuda()] + [torch.zeros((n, 7), device="cuda") for _ in range(steps)]
+        outs = [(torch.zeros((n, 98), device="cuda"), torch.zeros((n, 49), device="cuda")) for _ in range(steps)]
+        with frg.Context() as ctx:
+            plans = [ctx.plan_ragged(off, bufs[i], tqd, tu, outs[i][0], bufs[i + 1], outs[i][1]) for i in range(steps)]
+            torch.cuda.synchronize()
+            for i in range(steps):
+                if with_plain and i % 2 == 1:
+                    ctx.gradient(n, bufs[i], tqd, tu, outs[i][0], bufs[i + 1], outs[i][1],
+                                 torch.cuda.current_stream())
+                else:
+                    plans[i].launch(torch.cuda.current_stream())
+                if sync:
+                    torch.cuda.synchronize()
+            torch.cuda.synchronize()
+            for p in plans:
+                p.close()
+        return [t.cpu() for o in outs for t in o] + [b.cpu() for b in bufs]
+
+    for with_plain in (False, True):
+        unsynced, synced = chain(False, with_plain), chain(True, with_plain)
+        assert all(bool(torch.isfinite(t).all()) for t in synced)
+        for a, b in zip(unsynced, synced):
+            assert torch.equal(a, b)
+
+
 def test_plan_launches_capture_into_a_cuda_graph():
     """Plan launches captured into a CUDA graph (torch.cuda.graph) replay with
     the bits of direct launches."""
