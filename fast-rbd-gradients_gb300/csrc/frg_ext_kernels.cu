@@ -26,17 +26,24 @@ __global__ void __launch_bounds__(8 * 32)
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
-    dependent_launch_begin();
     const int wpc = blockDim.x >> 5, ntiles = (n + 31) / 32;
-    for (int tile = blockIdx.x * wpc + warp; tile < ntiles; tile += gridDim.x * wpc) {
+    auto knot = [&](int tile) {
         const long long g = static_cast<long long>(tile) * 32 + lane;
-        KnotPtrs kp{};
-        if (g < n) {
-            kp = KnotPtrs{q + kN * g, qd + kN * g, u + kN * g, dqdd ? dqdd + kDqddN * g : nullptr, qdd + kN * g,
-                          minv ? minv + kMinvN * g : nullptr, FEXT ? fext + kFextN * g : nullptr};
+        if (g >= n) return KnotPtrs{};
+        return KnotPtrs{q + kN * g, qd + kN * g, u + kN * g, dqdd ? dqdd + kDqddN * g : nullptr, qdd + kN * g,
+                        minv ? minv + kMinvN * g : nullptr, FEXT ? fext + kFextN * g : nullptr};
+    };
+    if (blockIdx.x * wpc + warp < ntiles) {  // the first tile's inputs into L2 while the work ahead finishes
+        const KnotPtrs kp = knot(blockIdx.x * wpc + warp);
+        prefetch_knot_inputs(kp);
+        if (FEXT && kp.fext) {
+            prefetch_l2(kp.fext);
+            prefetch_l2(kp.fext + kFextN - 1);
         }
-        process_tile<DAMP, MPC, false, FEXT, FDONLY>(ws, lane, kp);
     }
+    dependent_launch_begin();
+    for (int tile = blockIdx.x * wpc + warp; tile < ntiles; tile += gridDim.x * wpc)
+        process_tile<DAMP, MPC, false, FEXT, FDONLY>(ws, lane, knot(tile));
 }
 
 // Knot records [n][4N + N^2]: q, qd, u read from each record, q̈ and Minv
@@ -49,17 +56,18 @@ __global__ void __launch_bounds__(8 * 32) grad_knots_kernel(float *knots, float 
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem *ws = reinterpret_cast<WarpSmem *>(smem_raw) + warp;
-    dependent_launch_begin();
     const int wpc = blockDim.x >> 5, ntiles = (n + 31) / 32;
-    for (int tile = blockIdx.x * wpc + warp; tile < ntiles; tile += gridDim.x * wpc) {
+    auto knot = [&](int tile) {
         const long long g = static_cast<long long>(tile) * 32 + lane;
-        KnotPtrs kp{};
-        if (g < n) {
-            float *rec = knots + kKnotRecordFloats * g;
-            kp = KnotPtrs{rec, rec + kN, rec + 2 * kN, dqdd + kDqddN * g, rec + 3 * kN, rec + 4 * kN};
-        }
-        process_tile<DAMP, MPC>(ws, lane, kp);
-    }
+        if (g >= n) return KnotPtrs{};
+        float *rec = knots + kKnotRecordFloats * g;
+        return KnotPtrs{rec, rec + kN, rec + 2 * kN, dqdd + kDqddN * g, rec + 3 * kN, rec + 4 * kN};
+    };
+    if (blockIdx.x * wpc + warp < ntiles)  // the first tile's inputs into L2 while the work ahead finishes
+        prefetch_knot_inputs(knot(blockIdx.x * wpc + warp));
+    dependent_launch_begin();
+    for (int tile = blockIdx.x * wpc + warp; tile < ntiles; tile += gridDim.x * wpc)
+        process_tile<DAMP, MPC>(ws, lane, knot(tile));
 }
 
 // One thread per output float: A [n][4N^2] then B [n][2N^2].

@@ -27,9 +27,13 @@ __global__ void __launch_bounds__(kMaxWarps * 32)
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     GroupSmem *gs = reinterpret_cast<GroupSmem *>(smem_raw) + warp;
-    dependent_launch_begin();
     const long long items = (static_cast<long long>(n) + kGroupKnots - 1) / kGroupKnots;
     const int wpc = blockDim.x >> 5;
+    // the first slice's inputs into L2 while the work ahead finishes (prefetch_l2)
+    if (static_cast<long long>(blockIdx.x) * wpc + warp < items)
+        prefetch_knot_inputs(plain_group_knot(q, qd, u, dqdd, qdd, minv, n, static_cast<long long>(blockIdx.x) * wpc + warp,
+                                              lane));
+    dependent_launch_begin();
     for (long long it = static_cast<long long>(blockIdx.x) * wpc + warp; it < items;
          it += static_cast<long long>(gridDim.x) * wpc)
         process_group<DAMP, MPC>(gs, lane, plain_group_knot(q, qd, u, dqdd, qdd, minv, n, it, lane));
@@ -59,8 +63,23 @@ __device__ __forceinline__ void group_persistent(const Seg *segs, int nseg, cons
     extern __shared__ float4 smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     GroupSmem *gs = reinterpret_cast<GroupSmem *>(smem_raw) + warp;
-    dependent_launch_begin();
     const unsigned int items = static_cast<unsigned int>(ntiles) * 8u;
+    if constexpr (!SERVE) {
+        // the slice this warp is likely to draw first: its inputs into L2 while
+        // the work ahead finishes (descriptors are written only by host copies
+        // that the launch waits for in full; see grad_ragged_kernel)
+        const unsigned int first = blockIdx.x * (blockDim.x >> 5) + warp;
+        if (first < items) {
+            const int tile = static_cast<int>(first >> 3), slice = static_cast<int>(first & 7u);
+            const long long g = static_cast<long long>(tile) * 32 + slice * kGroupKnots + (lane >> 3);
+            if (g < segs[nseg].knot_begin) {
+                const Seg &sg = segs[segment_of(segs, nseg, tile_seg[tile], g)];
+                const long long i = g - sg.knot_begin;
+                prefetch_knot_inputs(KnotPtrs{sg.q + kN * i, sg.qd + kN * i, sg.u + kN * i, nullptr, nullptr, nullptr});
+            }
+        }
+    }
+    dependent_launch_begin();
     for (unsigned int ticket; next_ticket(items, counter, lane, ticket);) {
         const int tile = static_cast<int>(ticket >> 3), slice = static_cast<int>(ticket & 7u);
         const long long g = static_cast<long long>(tile) * 32 + slice * kGroupKnots + (lane >> 3);

@@ -65,16 +65,6 @@ __device__ __forceinline__ void relay_dqdd(const PlainArgs &a, int tile, int lan
     __syncwarp();
 }
 
-// A lane's knot inputs into L2 (before the wait on the work ahead; see
-// prefetch_l2).  Idle lanes (q == nullptr) issue nothing.
-__device__ __forceinline__ void prefetch_knot_inputs(const KnotPtrs &kp) {
-    if (kp.q) {
-        prefetch_l2(kp.q);
-        prefetch_l2(kp.qd);
-        prefetch_l2(kp.u);
-    }
-}
-
 // MINV_PACKED (host-buffer batches only): a.minv receives Minv's packed
 // upper triangle, kMinvPackedN floats per knot.
 template <bool DAMP, bool MPC, bool RELAY = false, bool MINV_PACKED = false>

@@ -29,6 +29,17 @@ __device__ __forceinline__ void prefetch_l2(const void *p) {
     asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
+// A lane's knot inputs (q, qd, u of a KnotPtrs) into L2; idle lanes
+// (q == nullptr) issue nothing.
+template <typename Ptrs>
+__device__ __forceinline__ void prefetch_knot_inputs(const Ptrs &kp) {
+    if (kp.q) {
+        prefetch_l2(kp.q);
+        prefetch_l2(kp.qd);
+        prefetch_l2(kp.u);
+    }
+}
+
 template <typename... KArgs, typename... Args>
 cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
                              Args... args) {

@@ -265,42 +265,48 @@ def test_back_to_back_launches_keep_stream_order():
 
 def test_plans_prepared_ahead_chain_without_synchronisation():
     """Plans prepared before the chain launch back to back, each reading the
-    previous plan's q̈ output as its joint angles: the persistent kernel brings
-    its first tile's inputs into L2 before it waits for the launch ahead of it,
-    and still reads the finished values.  Checked against the same chain with a
-    device synchronisation after every launch, also with plain launches
-    (which prefetch too) between the plans."""
+    previous launch's q̈ output as its joint angles: the kernels bring their
+    first tile's inputs into L2 before they wait for the launch ahead of them,
+    and still read the finished values.  Checked against the same chain with a
+    device synchronisation after every launch: plans alone, plans between
+    plain gradient and forward-dynamics launches (which prefetch too), and both
+    again in the latency mapping (8 lanes per knot)."""
     import torch
     h, off = frg.ragged_horizons(128, 8, 256, seed=60)
     n = int(off[-1])
     q, qd, u = frg.sample_knots(n, seed=61)
     tqd, tu = (torch.from_numpy(x).cuda() for x in (qd, u))
 
-    def chain(sync, with_plain):
-        steps = 6
+    def chain(sync, kinds, lanes):
+        steps = len(kinds)
         bufs = [torch.from_numpy(q).cuda()] + [torch.zeros((n, 7), device="cuda") for _ in range(steps)]
         outs = [(torch.zeros((n, 98), device="cuda"), torch.zeros((n, 49), device="cuda")) for _ in range(steps)]
         with frg.Context() as ctx:
-            plans = [ctx.plan_ragged(off, bufs[i], tqd, tu, outs[i][0], bufs[i + 1], outs[i][1]) for i in range(steps)]
+            ctx.set_lanes_per_knot(lanes)
+            plans = {i: ctx.plan_ragged(off, bufs[i], tqd, tu, outs[i][0], bufs[i + 1], outs[i][1])
+                     for i, k in enumerate(kinds) if k == "plan"}
             torch.cuda.synchronize()
-            for i in range(steps):
-                if with_plain and i % 2 == 1:
-                    ctx.gradient(n, bufs[i], tqd, tu, outs[i][0], bufs[i + 1], outs[i][1],
-                                 torch.cuda.current_stream())
+            st = torch.cuda.current_stream()
+            for i, k in enumerate(kinds):
+                if k == "plan":
+                    plans[i].launch(st)
+                elif k == "plain":
+                    ctx.gradient(n, bufs[i], tqd, tu, outs[i][0], bufs[i + 1], outs[i][1], st)
                 else:
-                    plans[i].launch(torch.cuda.current_stream())
+                    ctx.forward_dynamics(n, bufs[i], tqd, tu, bufs[i + 1], outs[i][1], stream=st)
                 if sync:
                     torch.cuda.synchronize()
             torch.cuda.synchronize()
-            for p in plans:
+            for p in plans.values():
                 p.close()
         return [t.cpu() for o in outs for t in o] + [b.cpu() for b in bufs]
 
-    for with_plain in (False, True):
-        unsynced, synced = chain(False, with_plain), chain(True, with_plain)
-        assert all(bool(torch.isfinite(t).all()) for t in synced)
-        for a, b in zip(unsynced, synced):
-            assert torch.equal(a, b)
+    for lanes in (1, 8):
+        for kinds in (["plan"] * 6, ["plan", "plain", "plan", "fd", "plan", "plain"]):
+            unsynced, synced = chain(False, kinds, lanes), chain(True, kinds, lanes)
+            assert all(bool(torch.isfinite(t).all()) for t in synced)
+            for a, b in zip(unsynced, synced):
+                assert torch.equal(a, b)
 
 
 def test_plan_launches_capture_into_a_cuda_graph():
