@@ -292,9 +292,11 @@ frg_status frg_gradient_ragged_noalloc(frg_ctx *ctx, int n_traj, const int64_t *
  * overlap on the device.  Every launch of the engine's gradient kernels uses
  * programmatic dependent launch: it may be scheduled while the previous work
  * on its stream finishes, and waits for that work to complete before reading
- * or writing anything, so stream order holds and back-to-back launches (solver
- * iterations, plan repeats) lose no time between them.  Plan launches can be
- * captured into a caller's CUDA graph like any kernel launch.
+ * its inputs or writing anything (before the wait it reads only its own launch
+ * descriptors and asks L2 to fetch its first inputs, a hint), so stream order
+ * holds and back-to-back launches (solver iterations, plan repeats) lose no
+ * time between them.  Plan launches can be captured into a caller's CUDA graph
+ * like any kernel launch.
  */
 frg_status frg_plan_create(frg_ctx *ctx, int n_traj, const frg_traj *trajs, frg_plan **out);
 frg_status frg_plan_create_ragged(frg_ctx *ctx, int n_traj, const int64_t *offsets, const float *q,
