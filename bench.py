@@ -7,7 +7,12 @@ through the full path (RNEA, Minv, q̈, dtau/dq, dtau/dqd, -Minv dtau) in FP32.
 
   value     knot-gradients/s of the batched form: one persistent launch over
             the ragged offset list (a plan launch per step), inputs resident
-            in HBM; 6 rotating input/output sets (~280 MB > 129 MB L2).
+            in HBM; 6 rotating input/output sets (~280 MB > 129 MB L2).  The
+            K steps are independent batches issued by one
+            frg_plan_launch_many call: even and odd steps on two streams, so
+            each launch's partial last wave overlaps the next batch.
+            single_stream: the same K launches one after another on one
+            stream.
   e2e       the same metric through the C ABI's host-buffer calls: H2D of
             q, qd, u from pinned memory, kernel, D2H of dqdd, qdd, Minv
             inside every timed step (frg_gradient_host_batches, two steps in
@@ -501,15 +506,33 @@ def run_frg(args):
         i += 1
         if i % 64 == 0:
             stream.synchronize()
+    # The K steps are K independent batches (the rotating sets).  Timed two
+    # ways: back to back on one stream (single_stream), and as one
+    # frg_plan_launch_many call, even and odd steps on two streams, so that a
+    # launch's partial last wave of tiles overlaps the next batch (value).
+    plans = [sets[i % ROTATING_SETS][4] for i in range(args.steps)]
+    if not args.profile:
+        ctx.plan_launch_many([s[4] for s in sets] * 2, stream)
+    barrier()
+    single_ms = timed(lambda i: sets[i % ROTATING_SETS][4].launch(stream), args.steps)
     barrier()
     t0 = time.perf_counter()
-    step_ms = timed(lambda i: sets[i % ROTATING_SETS][4].launch(stream), args.steps)
+    if args.profile:
+        step_ms = single_ms
+    else:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.plan_launch_many(plans, stream)
+        e1.record(stream)
+        stream.synchronize()
+        step_ms = [e0.elapsed_time(e1) / args.steps] * args.steps
     barrier()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     from frg import dist as fdist
     value, total_ms, _ = fdist.aggregate(sum(step_ms), n, args.steps, device=dev)
     ms_per_step = total_ms / args.steps
+    single_value, single_total_ms, _ = fdist.aggregate(sum(single_ms), n, args.steps, device=dev)
 
     # ---- parity of the timed launches' results: every knot of every rotating
     # set against the FP64 GPU verification build ----
@@ -598,7 +621,8 @@ def run_frg(args):
             "config": {
                 "workload": f"ragged mix: {n_traj} trajectories, horizons U{{{H_LO}..{H_HI}}} (seed {MIX_SEED}), "
                             f"{n} knots per rank, stored in shuffled order; one persistent launch over the "
-                            f"ragged trajectory list, one plan launch per step",
+                            f"ragged trajectory list, one plan launch per step; the steps are independent "
+                            f"batches, even and odd ones on two streams (frg_plan_launch_many)",
                 "knots_per_step": n, "l2": f"{ROTATING_SETS} rotating input/output sets "
                                             f"({ROTATING_SETS * n * BYTES_PER_KNOT / 1e6:.0f} MB > 129 MB L2)",
                 "launch_shape": tuning,
@@ -623,6 +647,9 @@ def run_frg(args):
                                       "host_link_frac": d2h_s * 392 / 616 / e2e_grad_s,
                                       "call": "frg_gradient_host_batches with qdd and minv NULL: dqdd alone "
                                               "returned, the output of the reference's Completely Fused call"}},
+            "single_stream": {"value": single_value, "unit": UNIT, "ms_per_step": single_total_ms / args.steps,
+                              "call": "the same K plan launches back to back on one stream (each launch starts "
+                                      "while the one before finishes, programmatic dependent launch)"},
             "plain_per_trajectory": {"value": plain_value, "unit": UNIT, "launches_per_step": n_traj,
                                      "ms_per_step": statistics.mean(plain_ms)},
             "batched_vs_plain": value / ws / plain_value,
@@ -639,7 +666,9 @@ def run_frg(args):
                                            "mix (NCU_MIX); the results stay dirty in L2 when the kernel ends",
                          "peak_source": f"{peaks_src} (MEASURED_PEAKS.json hbm_gbs)" if peaks_src == "measured"
                          else "fallback 6.8 TB/s", "bytes_per_knot": BYTES_PER_KNOT,
-                         "kernel": "grad_ragged_kernel", "launch_ms": launch_ms},
+                         "kernel": "grad_ragged_kernel", "launch_ms": launch_ms,
+                         "launch_ms_note": "time per batch with two independent batches in flight; "
+                                           "single_stream.ms_per_step is one launch after another"},
             "compute_roofline": {"bound": "fp32", "achieved": fp32_achieved, "unit": "TFLOP/s",
                                  "peak": fp32_peak, "frac": fp32_achieved / fp32_peak,
                                  "flop_per_knot": FLOP_PER_KNOT_REF,

@@ -7,6 +7,7 @@
 #include <new>
 #include <random>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "frg.h"
@@ -105,6 +106,41 @@ frg_status frg_plan_launch(frg_plan *plan, frg_stream stream) {
     DeviceGuard g(plan->ctx->device);
     if (!ok(plan->ctx, plan_launch(plan, reinterpret_cast<cudaStream_t>(stream)), "frg_plan_launch")) return FRG_ERR_CUDA;
     return FRG_OK;
+}
+
+frg_status frg_plan_launch_many(frg_ctx *ctx, int n_plans, frg_plan *const *plans, frg_stream stream) {
+    if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
+    if (n_plans < 0 || (n_plans > 0 && !plans)) {
+        frg_set_error(ctx, "frg_plan_launch_many: bad plan list");
+        return FRG_ERR_INVALID_ARGUMENT;
+    }
+    std::unordered_map<const frg_plan *, int> parity;  // position parity of each plan
+    for (int i = 0; i < n_plans; i++) {
+        if (!plans[i] || plans[i]->ctx != ctx) {
+            frg_set_error(ctx, "frg_plan_launch_many: plan " + std::to_string(i) + " is NULL or of another context");
+            return FRG_ERR_INVALID_ARGUMENT;
+        }
+        const auto it = parity.emplace(plans[i], i & 1).first;
+        if (it->second != (i & 1)) {
+            frg_set_error(ctx, "frg_plan_launch_many: plan " + std::to_string(i) +
+                                   " also appears at a position of the other parity; the two parities run concurrently");
+            return FRG_ERR_INVALID_ARGUMENT;
+        }
+    }
+    if (n_plans == 0) return FRG_OK;
+    DeviceGuard g(ctx->device);
+    cudaStream_t a = reinterpret_cast<cudaStream_t>(stream), b = ctx->pair_stream;
+    // b starts after the work queued on a so far; a continues after b's launches
+    if (!ok(ctx, cudaEventRecord(ctx->pair_fork, a), "frg_plan_launch_many fork") ||
+        !ok(ctx, cudaStreamWaitEvent(b, ctx->pair_fork, 0), "frg_plan_launch_many fork"))
+        return FRG_ERR_CUDA;
+    bool good = true;
+    for (int i = 0; good && i < n_plans; i++)
+        good = ok(ctx, plan_launch(plans[i], (i & 1) ? b : a), "frg_plan_launch_many launch");
+    // join even after a failed launch, so that a is never left ahead of b
+    const bool joined = ok(ctx, cudaEventRecord(ctx->pair_join, b), "frg_plan_launch_many join") &&
+                        ok(ctx, cudaStreamWaitEvent(a, ctx->pair_join, 0), "frg_plan_launch_many join");
+    return good && joined ? FRG_OK : FRG_ERR_CUDA;
 }
 
 int64_t frg_plan_knots(const frg_plan *plan) { return plan ? plan->nknots : 0; }

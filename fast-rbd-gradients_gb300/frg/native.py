@@ -31,7 +31,8 @@ EXPORTED = (
     "frg_options_default", "frg_status_string", "frg_create", "frg_destroy", "frg_last_error",
     "frg_set_launch_shape", "frg_get_launch_shape", "frg_set_lanes_per_knot", "frg_get_lanes_per_knot", "frg_gradient", "frg_gradient_host",
     "frg_gradient_per_trajectory", "frg_gradient_batched", "frg_gradient_ragged", "frg_plan_create",
-    "frg_plan_create_ragged", "frg_plan_launch", "frg_plan_knots", "frg_plan_destroy", "frg_autotune",
+    "frg_plan_create_ragged", "frg_plan_launch", "frg_plan_launch_many", "frg_plan_knots", "frg_plan_destroy",
+    "frg_autotune",
     "frg_host_alloc", "frg_host_free", "frg_gradient_ragged_noalloc", "frg_server_options_default",
     "frg_server_create", "frg_server_destroy", "frg_server_submit", "frg_server_poll", "frg_server_wait",
     "frg_server_wait_any", "frg_server_release", "frg_server_get_stats", "frg_gradient_fext",
@@ -127,6 +128,7 @@ def _declare(L):
         "frg_plan_create": (st, [vp, i32, ctypes.POINTER(Traj), ctypes.POINTER(vp)]),
         "frg_plan_create_ragged": (st, [vp, i32, ctypes.POINTER(i64), vp, vp, vp, vp, vp, vp, ctypes.POINTER(vp)]),
         "frg_plan_launch": (st, [vp, vp]),
+        "frg_plan_launch_many": (st, [vp, i32, ctypes.POINTER(vp), vp]),
         "frg_plan_knots": (i64, [vp]),
         "frg_plan_destroy": (None, [vp]),
         "frg_autotune": (st, [vp, i64, ctypes.POINTER(ctypes.c_double)]),
@@ -422,6 +424,14 @@ class Context:
         h = ctypes.c_void_p()
         self._check(lib().frg_plan_create(self._h, n, arr, ctypes.byref(h)), "frg_plan_create")
         return Plan(self, h)
+
+    def plan_launch_many(self, plans, stream=None):
+        """Independent plans, even and odd positions on two streams
+        (frg_plan_launch_many): a plan at an even position must not share
+        memory that either one writes with any plan at an odd position."""
+        arr = (ctypes.c_void_p * max(1, len(plans)))(*[p._h for p in plans])
+        self._check(lib().frg_plan_launch_many(self._h, len(plans), arr, _stream_ptr(stream)),
+                    "frg_plan_launch_many")
 
     def plan_ragged(self, offsets, q, qd, u, dqdd, qdd, minv):
         import numpy as np

@@ -309,6 +309,48 @@ def test_plans_prepared_ahead_chain_without_synchronisation():
                 assert torch.equal(a, b)
 
 
+def test_plan_launch_many_matches_single_launches():
+    """Independent plans with even and odd positions on two streams
+    (frg_plan_launch_many) give the bits of launching each plan alone; work
+    queued on the stream after the call sees every result without a host
+    synchronisation; a plan at both parities, or of another context, is
+    refused."""
+    import torch
+    with frg.Context() as ctx, frg.Context() as other:
+        sets = []
+        for i in range(4):
+            h, off = frg.ragged_horizons(48, 8, 256, seed=90 + i)
+            n = int(off[-1])
+            q, qd, u = frg.sample_knots(n, seed=190 + i)
+            ins = [torch.from_numpy(x).cuda() for x in (q, qd, u)]
+            alone, many = alloc(torch, n), alloc(torch, n)
+            sets.append((ctx.plan_ragged(off, *ins, *alone), ctx.plan_ragged(off, *ins, *many), alone, many, off, ins))
+        for p_alone, _, _, _, _, _ in sets:
+            p_alone.launch()
+        torch.cuda.synchronize()
+        for _, _, _, many, _, _ in sets:
+            for t in many:
+                t.fill_(float("nan"))
+        st = torch.cuda.current_stream()
+        ctx.plan_launch_many([s[1] for s in sets] * 3, st)  # plans 0, 2 even; 1, 3 odd; three times each
+        sums = [torch.stack([t.sum() for t in s[3]]) for s in sets]  # queued after the call, no host sync
+        torch.cuda.synchronize()
+        for (_, _, alone, many, _, _), sm in zip(sets, sums):
+            for a, b in zip(alone, many):
+                assert torch.equal(a, b)
+            assert torch.equal(sm, torch.stack([t.sum() for t in alone]))
+        ctx.plan_launch_many([], st)
+        with pytest.raises(frg.FrgError, match="other parity"):
+            ctx.plan_launch_many([sets[0][1], sets[1][1], sets[1][1]], st)  # plan 1 at positions 1 and 2
+        foreign = other.plan_ragged(sets[0][4], *sets[0][5], *alloc(torch, int(sets[0][4][-1])))
+        with pytest.raises(frg.FrgError, match="another context"):
+            ctx.plan_launch_many([sets[0][1], foreign], st)
+        foreign.close()
+        for s in sets:
+            s[0].close()
+            s[1].close()
+
+
 def test_plan_launches_capture_into_a_cuda_graph():
     """Plan launches captured into a CUDA graph (torch.cuda.graph) replay with
     the bits of direct launches."""
