@@ -16,7 +16,8 @@
 // times T trajectories of horizons U{8..256} stored in shuffled order in one
 // device buffer (as separately produced trajectories are) in the plain form
 // (one launch per trajectory, the only form the reference has), as one
-// batched persistent launch, and as a replayed plan (CUDA graph).
+// batched persistent launch, as a plan launch, and as two independent plans
+// (a second copy of the batch) in flight together (frg_plan_launch_many).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -98,21 +99,28 @@ int run_ragged(frg_ctx *ctx, int ntraj, int iters) {
     }
     std::vector<float> hin(21 * total);
     fill_knots(rng, total, hin.data(), hin.data() + 7 * total, hin.data() + 14 * total);
+    // two copies of the batch (inputs and outputs), the second for the
+    // independent plan that runs beside the first
     float *d = nullptr;
-    if (cudaMalloc(&d, sizeof(float) * 175 * total) != cudaSuccess) die(ctx, FRG_ERR_OUT_OF_MEMORY, "cudaMalloc");
+    if (cudaMalloc(&d, sizeof(float) * 2 * 175 * total) != cudaSuccess) die(ctx, FRG_ERR_OUT_OF_MEMORY, "cudaMalloc");
     cudaMemcpy(d, hin.data(), sizeof(float) * 21 * total, cudaMemcpyHostToDevice);
+    cudaMemcpy(d + 175 * total, hin.data(), sizeof(float) * 21 * total, cudaMemcpyHostToDevice);
     const size_t N = total;
-    std::vector<frg_traj> trajs(ntraj);
+    std::vector<frg_traj> trajs(ntraj), trajs2(ntraj);
     for (int t = 0; t < ntraj; t++) {
         const size_t m = mem[t];
         trajs[t] = frg_traj{h[t], d + 7 * m, d + 7 * N + 7 * m, d + 14 * N + 7 * m, d + 21 * N + 98 * m,
                             d + 119 * N + 7 * m, d + 126 * N + 49 * m};
+        float *d2 = d + 175 * N;
+        trajs2[t] = frg_traj{h[t], d2 + 7 * m, d2 + 7 * N + 7 * m, d2 + 14 * N + 7 * m, d2 + 21 * N + 98 * m,
+                             d2 + 119 * N + 7 * m, d2 + 126 * N + 49 * m};
     }
     cudaStream_t st;
     cudaStreamCreate(&st);
     frg_status s;
-    frg_plan *plan = nullptr;
+    frg_plan *plan = nullptr, *plan2 = nullptr;
     if ((s = frg_plan_create(ctx, ntraj, trajs.data(), &plan)) != FRG_OK) die(ctx, s, "frg_plan_create");
+    if ((s = frg_plan_create(ctx, ntraj, trajs2.data(), &plan2)) != FRG_OK) die(ctx, s, "frg_plan_create");
     const int n = static_cast<int>(total);
     auto plain = time_calls(iters, st, [&] {
         if ((s = frg_gradient_per_trajectory(ctx, ntraj, trajs.data(), st)) != FRG_OK)
@@ -124,11 +132,17 @@ int run_ragged(frg_ctx *ctx, int ntraj, int iters) {
     auto replay = time_calls(iters, st, [&] {
         if ((s = frg_plan_launch(plan, st)) != FRG_OK) die(ctx, s, "frg_plan_launch");
     });
+    frg_plan *pair[2] = {plan, plan2};
+    auto two = time_calls(iters, st, [&] {
+        if ((s = frg_plan_launch_many(ctx, 2, pair, st)) != FRG_OK) die(ctx, s, "frg_plan_launch_many");
+    });
     std::printf("%d trajectories, horizons U{8..256}, %d knots, stored in shuffled order\n", ntraj, n);
     print_stats("Plain - one launch per trajectory", n, plain);
     print_stats("Batched - one persistent launch", n, batched);
-    print_stats("Batched - plan replay (CUDA graph)", n, replay);
+    print_stats("Batched - plan launch", n, replay);
+    print_stats("Batched - two independent plans in flight (per call: both batches)", 2 * n, two);
     frg_plan_destroy(plan);
+    frg_plan_destroy(plan2);
     cudaStreamDestroy(st);
     cudaFree(d);
     return 0;

@@ -64,7 +64,8 @@ def test_time_frg_equivalence_point_matches_reference(golden, built_lib):
 def test_time_frg_ragged_and_batch_rows(built_lib):
     r = subprocess.run([TIME_FRG, "--ragged", "64", "--iters", "5"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
-    assert len(re.findall(r"^\[N:\d+\] (Plain|Batched)", r.stdout, re.M)) == 3
+    assert len(re.findall(r"^\[N:\d+\] (Plain|Batched)", r.stdout, re.M)) == 4
+    assert re.search(r"^\[N:\d+\] Batched - two independent plans in flight", r.stdout, re.M)
     r = subprocess.run([TIME_FRG, "--iters", "5", "16", "1000"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert len(re.findall(r"^\[N:(16|1000)\] Completely Fused", r.stdout, re.M)) == 4
