@@ -9,8 +9,9 @@ through the full path (RNEA, Minv, q̈, dtau/dq, dtau/dqd, -Minv dtau) in FP32.
             the ragged offset list (a plan launch per step), inputs resident
             in HBM; 6 rotating input/output sets (~280 MB > 129 MB L2).  The
             K steps are independent batches issued by one
-            frg_plan_launch_many call: even and odd steps on two streams, so
-            each launch's partial last wave overlaps the next batch.
+            frg_plan_launch_many call with three in flight (step i on stream
+            i mod 3), so each launch's partial last wave overlaps the next
+            batches.
             single_stream: the same K launches one after another on one
             stream.
   e2e       the same metric through the C ABI's host-buffer calls: H2D of
@@ -69,6 +70,7 @@ BYTES_PER_KNOT = 84 + 616          # algorithmic HBM bytes: q, qd, u in; dqdd, q
 D2H_PACKED = 392 + 28 + 112        # bytes per knot over the host link when Minv travels as its upper triangle
 FLOP_PER_KNOT_REF = 35257          # the reference's full path as written (op-counted)
 ROTATING_SETS = 6
+IN_FLIGHT = 3                      # independent batches in flight in the timed steps (divides ROTATING_SETS)
 
 
 def parse():
@@ -508,11 +510,13 @@ def run_frg(args):
             stream.synchronize()
     # The K steps are K independent batches (the rotating sets).  Timed two
     # ways: back to back on one stream (single_stream), and as one
-    # frg_plan_launch_many call, even and odd steps on two streams, so that a
-    # launch's partial last wave of tiles overlaps the next batch (value).
+    # frg_plan_launch_many call with IN_FLIGHT batches in flight (step i on
+    # stream i mod IN_FLIGHT), so that a launch's partial last wave of tiles
+    # overlaps the next batches (value).  ROTATING_SETS is a multiple of
+    # IN_FLIGHT, so each set always runs on the same stream.
     plans = [sets[i % ROTATING_SETS][4] for i in range(args.steps)]
     if not args.profile:
-        ctx.plan_launch_many([s[4] for s in sets] * 2, stream)
+        ctx.plan_launch_many([s[4] for s in sets] * 2, stream, IN_FLIGHT)
     barrier()
     single_ms = timed(lambda i: sets[i % ROTATING_SETS][4].launch(stream), args.steps)
     barrier()
@@ -522,7 +526,7 @@ def run_frg(args):
     else:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        ctx.plan_launch_many(plans, stream)
+        ctx.plan_launch_many(plans, stream, IN_FLIGHT)
         e1.record(stream)
         stream.synchronize()
         step_ms = [e0.elapsed_time(e1) / args.steps] * args.steps
@@ -622,7 +626,7 @@ def run_frg(args):
                 "workload": f"ragged mix: {n_traj} trajectories, horizons U{{{H_LO}..{H_HI}}} (seed {MIX_SEED}), "
                             f"{n} knots per rank, stored in shuffled order; one persistent launch over the "
                             f"ragged trajectory list, one plan launch per step; the steps are independent "
-                            f"batches, even and odd ones on two streams (frg_plan_launch_many)",
+                            f"batches, {IN_FLIGHT} in flight on {IN_FLIGHT} streams (frg_plan_launch_many)",
                 "knots_per_step": n, "l2": f"{ROTATING_SETS} rotating input/output sets "
                                             f"({ROTATING_SETS * n * BYTES_PER_KNOT / 1e6:.0f} MB > 129 MB L2)",
                 "launch_shape": tuning,
@@ -667,7 +671,7 @@ def run_frg(args):
                          "peak_source": f"{peaks_src} (MEASURED_PEAKS.json hbm_gbs)" if peaks_src == "measured"
                          else "fallback 6.8 TB/s", "bytes_per_knot": BYTES_PER_KNOT,
                          "kernel": "grad_ragged_kernel", "launch_ms": launch_ms,
-                         "launch_ms_note": "time per batch with two independent batches in flight; "
+                         "launch_ms_note": f"time per batch with {IN_FLIGHT} independent batches in flight; "
                                            "single_stream.ms_per_step is one launch after another"},
             "compute_roofline": {"bound": "fp32", "achieved": fp32_achieved, "unit": "TFLOP/s",
                                  "peak": fp32_peak, "frac": fp32_achieved / fp32_peak,

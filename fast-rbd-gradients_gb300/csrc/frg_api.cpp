@@ -217,9 +217,11 @@ frg_status frg_create(frg_ctx **out, const frg_options *opt_in) {
         !check(ctx, frg::init_f64_kernels(), "FP64 kernel set-up") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !check(ctx, cudaStreamCreateWithFlags(&ctx->io_stream2, cudaStreamNonBlocking), "cudaStreamCreate") ||
-        !check(ctx, cudaStreamCreateWithFlags(&ctx->pair_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
-        !check(ctx, cudaEventCreateWithFlags(&ctx->pair_fork, cudaEventDisableTiming), "cudaEventCreate") ||
-        !check(ctx, cudaEventCreateWithFlags(&ctx->pair_join, cudaEventDisableTiming), "cudaEventCreate") ||
+        !check(ctx, cudaStreamCreateWithFlags(&ctx->flight[0], cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !check(ctx, cudaStreamCreateWithFlags(&ctx->flight[1], cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !check(ctx, cudaStreamCreateWithFlags(&ctx->flight[2], cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !check(ctx, cudaEventCreateWithFlags(&ctx->flight_fork, cudaEventDisableTiming), "cudaEventCreate") ||
+        !check(ctx, cudaEventCreateWithFlags(&ctx->flight_join, cudaEventDisableTiming), "cudaEventCreate") ||
         !check(ctx, cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming), "cudaEventCreate") ||
         !check(ctx, cudaEventCreateWithFlags(&ctx->batch_done[0], cudaEventDisableTiming), "cudaEventCreate") ||
         !check(ctx, cudaEventCreateWithFlags(&ctx->batch_done[1], cudaEventDisableTiming), "cudaEventCreate") ||
@@ -244,7 +246,8 @@ void frg_destroy(frg_ctx *ctx) {
         DeviceGuard g(ctx->device);
         if (ctx->io_stream) cudaStreamSynchronize(ctx->io_stream);
         if (ctx->io_stream2) cudaStreamSynchronize(ctx->io_stream2);
-        if (ctx->pair_stream) cudaStreamSynchronize(ctx->pair_stream);
+        for (cudaStream_t f : ctx->flight)
+            if (f) cudaStreamSynchronize(f);
         if (ctx->scratch_done) cudaEventSynchronize(ctx->scratch_done);
         ctx->scratch.release();
         cudaFree(ctx->host_buf);
@@ -252,9 +255,10 @@ void frg_destroy(frg_ctx *ctx) {
         cudaFree(ctx->f64_buf);
         if (ctx->io_stream) cudaStreamDestroy(ctx->io_stream);
         if (ctx->io_stream2) cudaStreamDestroy(ctx->io_stream2);
-        if (ctx->pair_stream) cudaStreamDestroy(ctx->pair_stream);
-        if (ctx->pair_fork) cudaEventDestroy(ctx->pair_fork);
-        if (ctx->pair_join) cudaEventDestroy(ctx->pair_join);
+        for (cudaStream_t f : ctx->flight)
+            if (f) cudaStreamDestroy(f);
+        if (ctx->flight_fork) cudaEventDestroy(ctx->flight_fork);
+        if (ctx->flight_join) cudaEventDestroy(ctx->flight_join);
         if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
         for (cudaEvent_t e : ctx->batch_done)
             if (e) cudaEventDestroy(e);

@@ -69,10 +69,11 @@ struct frg_ctx {
     double *f64_buf = nullptr;          // frg_verify_f64 scratch (frg::kSlotN doubles per knot)
     size_t f64_buf_doubles = 0;
     cudaEvent_t scratch_done = nullptr;  // last launch that read `scratch`
-    // frg_plan_launch_many: the second launch stream, and the events that fork
-    // it from the caller's stream and join it back
-    cudaStream_t pair_stream = nullptr;
-    cudaEvent_t pair_fork = nullptr, pair_join = nullptr;
+    // frg_plan_launch_many: the extra launch streams, and the events that fork
+    // them from the caller's stream and join them back
+    static constexpr int kMaxInFlight = 4;
+    cudaStream_t flight[kMaxInFlight - 1] = {};
+    cudaEvent_t flight_fork = nullptr, flight_join = nullptr;
 };
 
 struct frg_plan {

@@ -108,38 +108,47 @@ frg_status frg_plan_launch(frg_plan *plan, frg_stream stream) {
     return FRG_OK;
 }
 
-frg_status frg_plan_launch_many(frg_ctx *ctx, int n_plans, frg_plan *const *plans, frg_stream stream) {
+frg_status frg_plan_launch_many(frg_ctx *ctx, int n_plans, frg_plan *const *plans, int in_flight,
+                                frg_stream stream) {
     if (!ctx) return FRG_ERR_INVALID_ARGUMENT;
-    if (n_plans < 0 || (n_plans > 0 && !plans)) {
-        frg_set_error(ctx, "frg_plan_launch_many: bad plan list");
+    if (n_plans < 0 || (n_plans > 0 && !plans) || in_flight < 1 || in_flight > frg_ctx::kMaxInFlight) {
+        frg_set_error(ctx, "frg_plan_launch_many: bad plan list or in_flight outside 1.." +
+                               std::to_string(frg_ctx::kMaxInFlight));
         return FRG_ERR_INVALID_ARGUMENT;
     }
-    std::unordered_map<const frg_plan *, int> parity;  // position parity of each plan
+    std::unordered_map<const frg_plan *, int> residue;  // the stream each plan runs on
     for (int i = 0; i < n_plans; i++) {
         if (!plans[i] || plans[i]->ctx != ctx) {
             frg_set_error(ctx, "frg_plan_launch_many: plan " + std::to_string(i) + " is NULL or of another context");
             return FRG_ERR_INVALID_ARGUMENT;
         }
-        const auto it = parity.emplace(plans[i], i & 1).first;
-        if (it->second != (i & 1)) {
+        const auto it = residue.emplace(plans[i], i % in_flight).first;
+        if (it->second != i % in_flight) {
             frg_set_error(ctx, "frg_plan_launch_many: plan " + std::to_string(i) +
-                                   " also appears at a position of the other parity; the two parities run concurrently");
+                                   " also appears at a position of another residue mod in_flight; those run "
+                                   "concurrently");
             return FRG_ERR_INVALID_ARGUMENT;
         }
     }
     if (n_plans == 0) return FRG_OK;
     DeviceGuard g(ctx->device);
-    cudaStream_t a = reinterpret_cast<cudaStream_t>(stream), b = ctx->pair_stream;
-    // b starts after the work queued on a so far; a continues after b's launches
-    if (!ok(ctx, cudaEventRecord(ctx->pair_fork, a), "frg_plan_launch_many fork") ||
-        !ok(ctx, cudaStreamWaitEvent(b, ctx->pair_fork, 0), "frg_plan_launch_many fork"))
+    cudaStream_t st[frg_ctx::kMaxInFlight] = {reinterpret_cast<cudaStream_t>(stream)};
+    for (int k = 1; k < in_flight; k++) st[k] = ctx->flight[k - 1];
+    // the extra streams start after the work queued on `stream` so far
+    if (in_flight > 1 && !ok(ctx, cudaEventRecord(ctx->flight_fork, st[0]), "frg_plan_launch_many fork"))
         return FRG_ERR_CUDA;
+    for (int k = 1; k < in_flight; k++)
+        if (!ok(ctx, cudaStreamWaitEvent(st[k], ctx->flight_fork, 0), "frg_plan_launch_many fork"))
+            return FRG_ERR_CUDA;
     bool good = true;
     for (int i = 0; good && i < n_plans; i++)
-        good = ok(ctx, plan_launch(plans[i], (i & 1) ? b : a), "frg_plan_launch_many launch");
-    // join even after a failed launch, so that a is never left ahead of b
-    const bool joined = ok(ctx, cudaEventRecord(ctx->pair_join, b), "frg_plan_launch_many join") &&
-                        ok(ctx, cudaStreamWaitEvent(a, ctx->pair_join, 0), "frg_plan_launch_many join");
+        good = ok(ctx, plan_launch(plans[i], st[i % in_flight]), "frg_plan_launch_many launch");
+    // `stream` continues after every extra stream's launches (joined even after
+    // a failed launch, so that no stream is left behind)
+    bool joined = true;
+    for (int k = 1; k < in_flight; k++)
+        joined = ok(ctx, cudaEventRecord(ctx->flight_join, st[k]), "frg_plan_launch_many join") &&
+                 ok(ctx, cudaStreamWaitEvent(st[0], ctx->flight_join, 0), "frg_plan_launch_many join") && joined;
     return good && joined ? FRG_OK : FRG_ERR_CUDA;
 }
 

@@ -128,7 +128,7 @@ def _declare(L):
         "frg_plan_create": (st, [vp, i32, ctypes.POINTER(Traj), ctypes.POINTER(vp)]),
         "frg_plan_create_ragged": (st, [vp, i32, ctypes.POINTER(i64), vp, vp, vp, vp, vp, vp, ctypes.POINTER(vp)]),
         "frg_plan_launch": (st, [vp, vp]),
-        "frg_plan_launch_many": (st, [vp, i32, ctypes.POINTER(vp), vp]),
+        "frg_plan_launch_many": (st, [vp, i32, ctypes.POINTER(vp), i32, vp]),
         "frg_plan_knots": (i64, [vp]),
         "frg_plan_destroy": (None, [vp]),
         "frg_autotune": (st, [vp, i64, ctypes.POINTER(ctypes.c_double)]),
@@ -425,12 +425,12 @@ class Context:
         self._check(lib().frg_plan_create(self._h, n, arr, ctypes.byref(h)), "frg_plan_create")
         return Plan(self, h)
 
-    def plan_launch_many(self, plans, stream=None):
-        """Independent plans, even and odd positions on two streams
-        (frg_plan_launch_many): a plan at an even position must not share
-        memory that either one writes with any plan at an odd position."""
+    def plan_launch_many(self, plans, stream=None, in_flight=2):
+        """Independent plans, several in flight (frg_plan_launch_many): plan
+        i runs on stream i mod in_flight; plans at positions of different
+        residues must not share memory that either one writes."""
         arr = (ctypes.c_void_p * max(1, len(plans)))(*[p._h for p in plans])
-        self._check(lib().frg_plan_launch_many(self._h, len(plans), arr, _stream_ptr(stream)),
+        self._check(lib().frg_plan_launch_many(self._h, len(plans), arr, int(in_flight), _stream_ptr(stream)),
                     "frg_plan_launch_many")
 
     def plan_ragged(self, offsets, q, qd, u, dqdd, qdd, minv):

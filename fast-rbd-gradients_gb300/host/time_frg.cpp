@@ -134,7 +134,7 @@ int run_ragged(frg_ctx *ctx, int ntraj, int iters) {
     });
     frg_plan *pair[2] = {plan, plan2};
     auto two = time_calls(iters, st, [&] {
-        if ((s = frg_plan_launch_many(ctx, 2, pair, st)) != FRG_OK) die(ctx, s, "frg_plan_launch_many");
+        if ((s = frg_plan_launch_many(ctx, 2, pair, 2, st)) != FRG_OK) die(ctx, s, "frg_plan_launch_many");
     });
     std::printf("%d trajectories, horizons U{8..256}, %d knots, stored in shuffled order\n", ntraj, n);
     print_stats("Plain - one launch per trajectory", n, plain);

@@ -304,22 +304,25 @@ frg_status frg_plan_create_ragged(frg_ctx *ctx, int n_traj, const int64_t *offse
                                   frg_plan **out);
 frg_status frg_plan_launch(frg_plan *plan, frg_stream stream);
 /*
- * Independent plans, two in flight: plans[i] is launched on `stream` for even
- * i and on a second stream of the context for odd i, so the two lists run side
- * by side.  A persistent launch's last wave of tiles leaves part of the GPU
- * idle; a launch of the other list fills it.  On the 512-trajectory mix this
- * takes a launch from 41 to 33 us.  Stream order is kept against everything
- * else: the launches wait for the work queued on `stream` before the call, and
- * work queued on `stream` after it waits for all n launches.  Any launch at an
- * even position may run at the same time as any launch at an odd position, so
- * the caller guarantees that those plans are independent: none writes memory
- * that another of the other parity reads or writes.  A plan may appear more
- * than once, but only at positions of one parity (else
- * FRG_ERR_INVALID_ARGUMENT): launches of one plan on both streams would share
- * its work counter.  All plans belong to ctx.  There is no counterpart in the
- * reference, whose launches are synchronous (time_GPU.cu:313-316).
+ * Independent plans, several in flight: plans[i] is launched on stream
+ * i mod in_flight, where stream 0 is `stream` and streams 1 to in_flight - 1
+ * belong to the context (in_flight 1 to 4), so the launches run side by side.
+ * A persistent launch's last wave of tiles leaves part of the GPU idle;
+ * launches on the other streams fill it.  On the 512-trajectory mix this takes
+ * a launch from 41 us to 33-34 us (two or three in flight).  Stream order is
+ * kept against everything else: the launches wait for the work queued on
+ * `stream` before the call, and work queued on `stream` after it waits for all
+ * n launches.  Launches on different streams may run at the same time in any
+ * combination, so the caller guarantees that plans at positions of different
+ * residues mod in_flight are independent: none writes memory that another
+ * reads or writes.  A plan may appear more than once, but only at positions
+ * of one residue (else FRG_ERR_INVALID_ARGUMENT): launches of one plan on two
+ * streams would share its work counter.  All plans belong to ctx.  There is
+ * no counterpart in the reference, whose launches are synchronous
+ * (time_GPU.cu:313-316).
  */
-frg_status frg_plan_launch_many(frg_ctx *ctx, int n_plans, frg_plan *const *plans, frg_stream stream);
+frg_status frg_plan_launch_many(frg_ctx *ctx, int n_plans, frg_plan *const *plans, int in_flight,
+                                frg_stream stream);
 int64_t frg_plan_knots(const frg_plan *plan);
 void frg_plan_destroy(frg_plan *plan);
 

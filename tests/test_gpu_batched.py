@@ -310,11 +310,11 @@ def test_plans_prepared_ahead_chain_without_synchronisation():
 
 
 def test_plan_launch_many_matches_single_launches():
-    """Independent plans with even and odd positions on two streams
-    (frg_plan_launch_many) give the bits of launching each plan alone; work
-    queued on the stream after the call sees every result without a host
-    synchronisation; a plan at both parities, or of another context, is
-    refused."""
+    """Independent plans several in flight (frg_plan_launch_many: plan i on
+    stream i mod in_flight) give the bits of launching each plan alone, for
+    1 to 4 in flight; work queued on the stream after the call sees every
+    result without a host synchronisation; a plan at two residues, an
+    in_flight outside 1..4, or a plan of another context is refused."""
     import torch
     with frg.Context() as ctx, frg.Context() as other:
         sets = []
@@ -328,20 +328,27 @@ def test_plan_launch_many_matches_single_launches():
         for p_alone, _, _, _, _, _ in sets:
             p_alone.launch()
         torch.cuda.synchronize()
-        for _, _, _, many, _, _ in sets:
-            for t in many:
-                t.fill_(float("nan"))
         st = torch.cuda.current_stream()
-        ctx.plan_launch_many([s[1] for s in sets] * 3, st)  # plans 0, 2 even; 1, 3 odd; three times each
-        sums = [torch.stack([t.sum() for t in s[3]]) for s in sets]  # queued after the call, no host sync
-        torch.cuda.synchronize()
-        for (_, _, alone, many, _, _), sm in zip(sets, sums):
-            for a, b in zip(alone, many):
-                assert torch.equal(a, b)
-            assert torch.equal(sm, torch.stack([t.sum() for t in alone]))
+        for in_flight in (1, 2, 3, 4):
+            k = 3 if in_flight == 3 else 4  # plans per period: each plan keeps one residue
+            for _, _, _, many, _, _ in sets:
+                for t in many:
+                    t.fill_(float("nan"))
+            ctx.plan_launch_many([s[1] for s in sets[:k]] * 3, st, in_flight)
+            sums = [torch.stack([t.sum() for t in s[3]]) for s in sets[:k]]  # queued after the call, no host sync
+            torch.cuda.synchronize()
+            for (_, _, alone, many, _, _), sm in zip(sets[:k], sums):
+                for a, b in zip(alone, many):
+                    assert torch.equal(a, b), in_flight
+                assert torch.equal(sm, torch.stack([t.sum() for t in alone])), in_flight
         ctx.plan_launch_many([], st)
-        with pytest.raises(frg.FrgError, match="other parity"):
-            ctx.plan_launch_many([sets[0][1], sets[1][1], sets[1][1]], st)  # plan 1 at positions 1 and 2
+        with pytest.raises(frg.FrgError, match="another residue"):
+            ctx.plan_launch_many([sets[0][1], sets[1][1], sets[1][1]], st, 2)  # plan 1 at positions 1 and 2
+        with pytest.raises(frg.FrgError, match="another residue"):
+            ctx.plan_launch_many([sets[0][1], sets[1][1]] * 2, st, 3)  # plan 0 at positions 0 and 2
+        for bad in (0, 5):
+            with pytest.raises(frg.FrgError, match="in_flight"):
+                ctx.plan_launch_many([sets[0][1]], st, bad)
         foreign = other.plan_ragged(sets[0][4], *sets[0][5], *alloc(torch, int(sets[0][4][-1])))
         with pytest.raises(frg.FrgError, match="another context"):
             ctx.plan_launch_many([sets[0][1], foreign], st)
