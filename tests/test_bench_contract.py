@@ -71,3 +71,19 @@ def test_peaks_are_read_from_the_measured_file():
     if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
         assert src == "measured"
     assert float(peaks["hbm_gbs"]) > 0
+
+
+def test_rotating_sets_keep_one_stream_each():
+    """The timed steps go through frg_plan_launch_many with IN_FLIGHT streams,
+    step i on stream i mod IN_FLIGHT over set i mod ROTATING_SETS: every set
+    must land on one stream only (the call refuses a plan at two residues),
+    and the sets must still exceed L2 together."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert 1 <= bench.IN_FLIGHT <= 4
+    assert bench.ROTATING_SETS % bench.IN_FLIGHT == 0
+    residues = {}
+    for i in range(100):
+        residues.setdefault(i % bench.ROTATING_SETS, set()).add(i % bench.IN_FLIGHT)
+    assert all(len(r) == 1 for r in residues.values())
+    assert bench.ROTATING_SETS * 66809 * bench.BYTES_PER_KNOT > 129e6
